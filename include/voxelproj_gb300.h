@@ -1,0 +1,118 @@
+/*
+ * voxelproj_gb300 — C ABI of the exact-trapezoid parallel-beam projector
+ * pair for NVIDIA GB300 (sm_103a).
+ *
+ * The four projector entry points replace the reference's pybind functions
+ * voxelproj._CU.forward_z0 / backward_z0 / forward_z2 / backward_z2
+ * (voxelproj/csrc/voxelproj.cpp:15-33, implemented in
+ * voxelproj/csrc/projectors.cu:34-299).  Argument meaning follows them:
+ *
+ *   forward_*(in = x, out = y, angles)    y += A x
+ *   backward_*(in = y, out = x, angles)   x += A^T y
+ *
+ * Layouts (row-major, float32, contiguous):
+ *   z_order 0: x (SY, SX, Hx), y (n_ang, PX, Hy)   heights contiguous
+ *   z_order 2: x (Hx, SY, SX), y (Hy, n_ang, PX)   columns / bins contiguous
+ *
+ * The volume grid (SY, SX) is taken from x and the detector (n_ang, PX) from
+ * y, as the reference takes them from whichever of in/out holds them.  Only
+ * heights h < min(Hx, Hy) are computed: the reference reads heights past the
+ * input's extent as zero through its border-mode texture, which leaves those
+ * output heights unchanged, and so does this library.
+ *
+ * Semantics kept from the reference: results are ACCUMULATED into the output
+ * (`out += ...`, sp_forward_z0.cuh:167,180; sp_backward_z0.cuh:98); angles are
+ * radians and only the first n_ang entries are read.
+ *
+ * Differences from the reference, all of them additions:
+ *   - any number of angles (the reference adjoint is limited to 512);
+ *   - every argument is validated and an error code is returned instead of
+ *     launching on bad input (the reference checked only `in`);
+ *   - work is enqueued on the caller's stream and never synchronises (the
+ *     reference ran on the legacy default stream and synchronised through
+ *     cudaFreeArray);
+ *   - no per-call allocation or staging copy of the input.
+ *
+ * All pointers are device pointers on the current CUDA device.  `stream` is a
+ * cudaStream_t (NULL = legacy default stream).
+ */
+#ifndef VOXELPROJ_GB300_H
+#define VOXELPROJ_GB300_H
+
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define VP_API __attribute__((visibility("default")))
+#else
+#define VP_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes. */
+#define VP_OK 0
+#define VP_ERR_NULL_POINTER 1   /* a pointer is NULL while its array is non-empty */
+#define VP_ERR_BAD_SHAPE 2      /* negative or too large dimension */
+#define VP_ERR_ANGLES 3         /* fewer angles than the angle extent of y */
+#define VP_ERR_CUDA 4           /* a CUDA runtime call failed; see vp_last_cuda_error() */
+#define VP_ERR_BAD_FLAGS 5      /* unknown bit in `flags` */
+#define VP_ERR_BAD_Z_ORDER 6    /* z_order other than 0 or 2 */
+
+/* Flags. */
+#define VP_FLAG_TRIG_PRECISE 1  /* accurate sincosf / IEEE division for the per-angle
+                                   constants; default is the hardware approximations
+                                   that the reference's --use_fast_math build uses */
+
+/* Library version, major*10000 + minor*100 + patch. */
+VP_API int vp_version(void);
+
+/* Static text for a status code. */
+VP_API const char* vp_error_string(int status);
+
+/* The cudaError_t of the last VP_ERR_CUDA returned on this host thread. */
+VP_API int vp_last_cuda_error(void);
+
+/* Number of kernels this library has launched in this process (all threads).
+ * No counterpart in the reference; lets callers and benchmarks see how many
+ * GPU launches a sequence of calls issued. */
+VP_API uint64_t vp_launch_count(void);
+
+/* y += A x, z_order 0.  x (x0=SY, x1=SX, x2=Hx), y (y0=n_ang, y1=PX, y2=Hy).
+ * Replaces voxelproj._CU.forward_z0 (voxelproj/csrc/projectors.cu:34-104). */
+VP_API int vp_forward_z0(const float* x, int64_t x0, int64_t x1, int64_t x2,
+                  float* y, int64_t y0, int64_t y1, int64_t y2,
+                  const float* angles, int64_t n_angles, int flags, void* stream);
+
+/* x += A^T y, z_order 0.  y (y0=n_ang, y1=PX, y2=Hy), x (x0=SY, x1=SX, x2=Hx).
+ * Replaces voxelproj._CU.backward_z0 (voxelproj/csrc/projectors.cu:106-169). */
+VP_API int vp_backward_z0(const float* y, int64_t y0, int64_t y1, int64_t y2,
+                   float* x, int64_t x0, int64_t x1, int64_t x2,
+                   const float* angles, int64_t n_angles, int flags, void* stream);
+
+/* y += A x, z_order 2.  x (x0=Hx, x1=SY, x2=SX), y (y0=Hy, y1=n_ang, y2=PX).
+ * Replaces voxelproj._CU.forward_z2 (voxelproj/csrc/projectors.cu:171-234). */
+VP_API int vp_forward_z2(const float* x, int64_t x0, int64_t x1, int64_t x2,
+                  float* y, int64_t y0, int64_t y1, int64_t y2,
+                  const float* angles, int64_t n_angles, int flags, void* stream);
+
+/* x += A^T y, z_order 2.  y (y0=Hy, y1=n_ang, y2=PX), x (x0=Hx, x1=SY, x2=SX).
+ * Replaces voxelproj._CU.backward_z2 (voxelproj/csrc/projectors.cu:236-299). */
+VP_API int vp_backward_z2(const float* y, int64_t y0, int64_t y1, int64_t y2,
+                   float* x, int64_t x0, int64_t x1, int64_t x2,
+                   const float* angles, int64_t n_angles, int flags, void* stream);
+
+/* z_order dispatch, as voxelproj.wrappers.forward/backward select a kernel by
+ * z_order (voxelproj/wrappers.py:44-47, :92-95); dims as for the
+ * matching entry point above. */
+VP_API int vp_forward(const float* x, const int64_t x_dims[3], float* y, const int64_t y_dims[3],
+               const float* angles, int64_t n_angles, int z_order, int flags, void* stream);
+VP_API int vp_backward(const float* y, const int64_t y_dims[3], float* x, const int64_t x_dims[3],
+                const float* angles, int64_t n_angles, int z_order, int flags, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* VOXELPROJ_GB300_H */

@@ -1,0 +1,78 @@
+"""The C-ABI library without a GPU: it loads, exports every function that
+include/*.h declares, and rejects bad arguments before any CUDA call."""
+
+from __future__ import annotations
+
+import ctypes
+import re
+from pathlib import Path
+
+import pytest
+
+from voxelproj_gb300 import _lib
+
+ROOT = Path(__file__).resolve().parent.parent
+
+
+def declared_functions():
+    names = []
+    for h in sorted((ROOT / "include").glob("*.h")):
+        text = h.read_text()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        names += re.findall(r"\bVP_API\s+[\w\s\*]+?\b(vp_\w+)\s*\(", text)
+    return names
+
+
+def test_header_declares_entry_points():
+    names = declared_functions()
+    for required in ["vp_forward_z0", "vp_backward_z0", "vp_forward_z2", "vp_backward_z2",
+                     "vp_forward", "vp_backward", "vp_error_string", "vp_version"]:
+        assert required in names
+
+
+@pytest.mark.parametrize("name", declared_functions())
+def test_library_exports_declared_symbol(name):
+    lib = ctypes.CDLL(str(_lib.LIB_PATH))
+    assert hasattr(lib, name), f"{name} declared in include/ but not exported"
+
+
+def test_binding_covers_header():
+    assert set(declared_functions()) <= set(_lib.SIGNATURES)
+
+
+def test_status_strings():
+    for code in range(0, 7):
+        assert _lib.LIB.vp_error_string(code)
+    assert b"unknown" in _lib.LIB.vp_error_string(99)
+
+
+DUMMY = ctypes.c_void_p(0x1000)  # never dereferenced: validation fails first
+
+
+@pytest.mark.parametrize("fn", ["vp_forward_z0", "vp_backward_z0", "vp_forward_z2",
+                                "vp_backward_z2"])
+def test_validation_errors_without_gpu(fn):
+    f = getattr(_lib.LIB, fn)
+    good = (4, 5, 6)
+    # negative dimension
+    assert f(DUMMY, -1, 5, 6, DUMMY, *good, DUMMY, 10, 0, None) == _lib.VP_ERR_BAD_SHAPE
+    # too few angles for the sinogram's angle extent (7 angles, 6 given)
+    y_dims = (7, 5, 6) if fn.endswith("z0") else (6, 7, 5)
+    args = (DUMMY, *good, DUMMY, *y_dims) if "forward" in fn else (DUMMY, *y_dims, DUMMY, *good)
+    assert f(*args, DUMMY, 6, 0, None) == _lib.VP_ERR_ANGLES
+    # unknown flag bits
+    assert f(DUMMY, *good, DUMMY, *good, DUMMY, 10, 1 << 7, None) == _lib.VP_ERR_BAD_FLAGS
+    # null data pointer for a non-empty array
+    assert f(None, *good, DUMMY, *good, DUMMY, 10, 0, None) == _lib.VP_ERR_NULL_POINTER
+    assert f(DUMMY, *good, DUMMY, *good, None, 10, 0, None) == _lib.VP_ERR_NULL_POINTER
+    # empty problems succeed without touching the device
+    assert f(None, 0, 0, 0, None, 0, 0, 0, None, 0, 0, None) == _lib.VP_OK
+    assert f(DUMMY, 4, 5, 0, DUMMY, 4, 5, 0, DUMMY, 10, 0, None) == _lib.VP_OK
+
+
+def test_dispatch_rejects_bad_z_order():
+    dims = (ctypes.c_int64 * 3)(4, 5, 6)
+    assert _lib.LIB.vp_forward(DUMMY, dims, DUMMY, dims, DUMMY, 10, 1, 0, None) == \
+        _lib.VP_ERR_BAD_Z_ORDER
+    assert _lib.LIB.vp_backward(DUMMY, dims, DUMMY, dims, DUMMY, 10, 3, 0, None) == \
+        _lib.VP_ERR_BAD_Z_ORDER

@@ -1,0 +1,69 @@
+"""ctypes binding of the CUDA C-ABI library ``lib/libvoxelproj_gb300.so``.
+
+The signatures mirror ``include/voxelproj_gb300.h``.  There is no fallback:
+if the library is missing, importing the package fails with instructions to
+build it.
+"""
+
+from __future__ import annotations
+
+import ctypes
+from pathlib import Path
+
+LIB_PATH = Path(__file__).resolve().parent / "lib" / "libvoxelproj_gb300.so"
+
+VP_OK = 0
+VP_ERR_NULL_POINTER = 1
+VP_ERR_BAD_SHAPE = 2
+VP_ERR_ANGLES = 3
+VP_ERR_CUDA = 4
+VP_ERR_BAD_FLAGS = 5
+VP_ERR_BAD_Z_ORDER = 6
+
+VP_FLAG_TRIG_PRECISE = 1
+
+_P = ctypes.c_void_p
+_I64 = ctypes.c_int64
+_I = ctypes.c_int
+
+# name -> (restype, argtypes)
+SIGNATURES = {
+    "vp_version": (_I, []),
+    "vp_error_string": (ctypes.c_char_p, [_I]),
+    "vp_last_cuda_error": (_I, []),
+    "vp_launch_count": (ctypes.c_uint64, []),
+    "vp_forward_z0": (_I, [_P, _I64, _I64, _I64, _P, _I64, _I64, _I64, _P, _I64, _I, _P]),
+    "vp_backward_z0": (_I, [_P, _I64, _I64, _I64, _P, _I64, _I64, _I64, _P, _I64, _I, _P]),
+    "vp_forward_z2": (_I, [_P, _I64, _I64, _I64, _P, _I64, _I64, _I64, _P, _I64, _I, _P]),
+    "vp_backward_z2": (_I, [_P, _I64, _I64, _I64, _P, _I64, _I64, _I64, _P, _I64, _I, _P]),
+    "vp_forward": (_I, [_P, _P, _P, _P, _P, _I64, _I, _I, _P]),
+    "vp_backward": (_I, [_P, _P, _P, _P, _P, _I64, _I, _I, _P]),
+}
+
+
+def _load() -> ctypes.CDLL:
+    if not LIB_PATH.exists():
+        raise ImportError(
+            f"voxelproj_gb300: native library {LIB_PATH} is missing; build it with "
+            "`python voxelproj_gb300/build.py` (needs nvcc)")
+    L = ctypes.CDLL(str(LIB_PATH))
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    return L
+
+
+LIB = _load()
+
+
+def error_text(status: int) -> str:
+    msg = LIB.vp_error_string(status).decode()
+    if status == VP_ERR_CUDA:
+        msg += f" (cudaError {LIB.vp_last_cuda_error()})"
+    return msg
+
+
+def check(status: int, what: str) -> None:
+    if status != VP_OK:
+        raise RuntimeError(f"voxelproj_gb300.{what}: {error_text(status)}")

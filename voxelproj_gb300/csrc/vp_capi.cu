@@ -1,0 +1,161 @@
+// C ABI: argument validation, geometry setup and dispatch to the kernels.
+// The reference's host launchers (voxelproj/csrc/projectors.cu:34-299) also
+// copied the input into a cudaArray and bound a texture on every call; none
+// of that exists here, so a call is validation plus one kernel launch.
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <cstdint>
+
+#include "../../include/voxelproj_gb300.h"
+#include "vp_common.cuh"
+#include "vp_launch.h"
+
+namespace {
+
+thread_local int g_last_cuda_error = 0;
+std::atomic<uint64_t> g_launches{0};
+
+constexpr int64_t kMaxDim = (int64_t)1 << 30;
+// fp_z0 packs the voxel index (yi*SX + xi) with 3 tag bits into an int.
+constexpr int64_t kMaxVoxelsPerSlice = (int64_t)1 << 28;
+
+int check_flags(int flags) { return (flags & ~VP_FLAG_TRIG_PRECISE) ? VP_ERR_BAD_FLAGS : VP_OK; }
+
+bool dims_ok(int64_t a, int64_t b, int64_t c) {
+  return a >= 0 && b >= 0 && c >= 0 && a < kMaxDim && b < kMaxDim && c < kMaxDim;
+}
+
+// Builds the geometry from x's (SY, SX, Hx) and y's (n_ang, PX, Hy) and
+// validates pointers and the angle count.  Sets *empty when there is no work.
+int make_geom(const void* xp, int64_t SY, int64_t SX, int64_t Hx, const void* yp, int64_t n_ang,
+              int64_t PX, int64_t Hy, const float* angles, int64_t n_angles, int flags,
+              vp::Geom* g, bool* empty) {
+  if (int s = check_flags(flags)) return s;
+  if (!dims_ok(SY, SX, Hx) || !dims_ok(n_ang, PX, Hy)) return VP_ERR_BAD_SHAPE;
+  if (SY * SX >= kMaxVoxelsPerSlice) return VP_ERR_BAD_SHAPE;
+  if (n_angles < 0) return VP_ERR_ANGLES;
+  const int64_t H = Hx < Hy ? Hx : Hy;
+  *empty = (SY == 0 || SX == 0 || n_ang == 0 || PX == 0 || H == 0);
+  if (n_ang > 0 && n_angles < n_ang) return VP_ERR_ANGLES;
+  if ((SY * SX * Hx > 0 && xp == nullptr) || (n_ang * PX * Hy > 0 && yp == nullptr) ||
+      (n_ang > 0 && angles == nullptr))
+    return VP_ERR_NULL_POINTER;
+  g->SY = (int)SY;
+  g->SX = (int)SX;
+  g->n_ang = (int)n_ang;
+  g->PX = (int)PX;
+  g->H = (int)H;
+  g->Hx = (int)Hx;
+  g->Hy = (int)Hy;
+  g->xcent = 0.5f * (float)(SX - 1);
+  g->ycent = 0.5f * (float)(SY - 1);
+  g->pcent = 0.5f * (float)(PX - 1);
+  g->trig = (flags & VP_FLAG_TRIG_PRECISE) ? vp::TRIG_PRECISE : vp::TRIG_REF;
+  return VP_OK;
+}
+
+int finish(cudaError_t e, int launches) {
+  g_launches.fetch_add((uint64_t)launches, std::memory_order_relaxed);
+  if (e != cudaSuccess) {
+    g_last_cuda_error = (int)e;
+    return VP_ERR_CUDA;
+  }
+  return VP_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int vp_version(void) { return 100; }
+
+const char* vp_error_string(int status) {
+  switch (status) {
+    case VP_OK: return "ok";
+    case VP_ERR_NULL_POINTER: return "null pointer for a non-empty array";
+    case VP_ERR_BAD_SHAPE: return "invalid array shape";
+    case VP_ERR_ANGLES: return "fewer angles than the angle extent of the sinogram";
+    case VP_ERR_CUDA: return "CUDA runtime error";
+    case VP_ERR_BAD_FLAGS: return "unknown flag bits";
+    case VP_ERR_BAD_Z_ORDER: return "z_order must be 0 or 2";
+    default: return "unknown status";
+  }
+}
+
+int vp_last_cuda_error(void) { return g_last_cuda_error; }
+
+uint64_t vp_launch_count(void) { return g_launches.load(std::memory_order_relaxed); }
+
+int vp_forward_z0(const float* x, int64_t x0, int64_t x1, int64_t x2, float* y, int64_t y0,
+                  int64_t y1, int64_t y2, const float* angles, int64_t n_angles, int flags,
+                  void* stream) {
+  vp::Geom g;
+  bool empty = false;
+  if (int s = make_geom(x, x0, x1, x2, y, y0, y1, y2, angles, n_angles, flags, &g, &empty))
+    return s;
+  if (empty) return VP_OK;
+  return finish(vp::launch_forward_z0(x, y, angles, g, (cudaStream_t)stream),
+                vp::launches_forward_z0(g));
+}
+
+int vp_backward_z0(const float* y, int64_t y0, int64_t y1, int64_t y2, float* x, int64_t x0,
+                   int64_t x1, int64_t x2, const float* angles, int64_t n_angles, int flags,
+                   void* stream) {
+  vp::Geom g;
+  bool empty = false;
+  if (int s = make_geom(x, x0, x1, x2, y, y0, y1, y2, angles, n_angles, flags, &g, &empty))
+    return s;
+  if (empty) return VP_OK;
+  return finish(vp::launch_backward_z0(y, x, angles, g, (cudaStream_t)stream), 1);
+}
+
+int vp_forward_z2(const float* x, int64_t x0, int64_t x1, int64_t x2, float* y, int64_t y0,
+                  int64_t y1, int64_t y2, const float* angles, int64_t n_angles, int flags,
+                  void* stream) {
+  vp::Geom g;
+  bool empty = false;
+  // z_order 2: x (Hx, SY, SX), y (Hy, n_ang, PX)
+  if (int s = make_geom(x, x1, x2, x0, y, y1, y2, y0, angles, n_angles, flags, &g, &empty))
+    return s;
+  if (empty) return VP_OK;
+  return finish(vp::launch_forward_z2(x, y, angles, g, (cudaStream_t)stream),
+                vp::launches_forward_z2(g));
+}
+
+int vp_backward_z2(const float* y, int64_t y0, int64_t y1, int64_t y2, float* x, int64_t x0,
+                   int64_t x1, int64_t x2, const float* angles, int64_t n_angles, int flags,
+                   void* stream) {
+  vp::Geom g;
+  bool empty = false;
+  if (int s = make_geom(x, x1, x2, x0, y, y1, y2, y0, angles, n_angles, flags, &g, &empty))
+    return s;
+  if (empty) return VP_OK;
+  return finish(vp::launch_backward_z2(y, x, angles, g, (cudaStream_t)stream), 1);
+}
+
+int vp_forward(const float* x, const int64_t x_dims[3], float* y, const int64_t y_dims[3],
+               const float* angles, int64_t n_angles, int z_order, int flags, void* stream) {
+  if (x_dims == nullptr || y_dims == nullptr) return VP_ERR_NULL_POINTER;
+  if (z_order == 0)
+    return vp_forward_z0(x, x_dims[0], x_dims[1], x_dims[2], y, y_dims[0], y_dims[1], y_dims[2],
+                         angles, n_angles, flags, stream);
+  if (z_order == 2)
+    return vp_forward_z2(x, x_dims[0], x_dims[1], x_dims[2], y, y_dims[0], y_dims[1], y_dims[2],
+                         angles, n_angles, flags, stream);
+  return VP_ERR_BAD_Z_ORDER;
+}
+
+int vp_backward(const float* y, const int64_t y_dims[3], float* x, const int64_t x_dims[3],
+                const float* angles, int64_t n_angles, int z_order, int flags, void* stream) {
+  if (x_dims == nullptr || y_dims == nullptr) return VP_ERR_NULL_POINTER;
+  if (z_order == 0)
+    return vp_backward_z0(y, y_dims[0], y_dims[1], y_dims[2], x, x_dims[0], x_dims[1], x_dims[2],
+                          angles, n_angles, flags, stream);
+  if (z_order == 2)
+    return vp_backward_z2(y, y_dims[0], y_dims[1], y_dims[2], x, x_dims[0], x_dims[1], x_dims[2],
+                          angles, n_angles, flags, stream);
+  return VP_ERR_BAD_Z_ORDER;
+}
+
+}  // extern "C"

@@ -1,0 +1,190 @@
+// Shared device math of the exact-trapezoid parallel-beam projector pair.
+//
+// Geometry (reference voxelproj, sp_backward_z0.cuh:24-26 and :84): voxel and
+// detector pitch are 1; the volume centre is ((SX-1)/2, (SY-1)/2), the
+// detector centre (PX-1)/2, and voxel (xi, yi) lands on detector coordinate
+//     xp = (xi - xcent) * cos(phi) + (yi - ycent) * sin(phi) + pcent.
+// A unit voxel seen at angle phi is a trapezoid of area one with plateau
+// half-width a = min(|c-s|, |c+s|)/2, base half-width b = max(...)/2 and
+// height 1/(a+b) (sp_backward_z0.cuh:45-58).  Because b <= sqrt(2)/2 it covers
+// at most the three bins round(xp)-1, round(xp), round(xp)+1 (:85-95), whose
+// weights are differences of the trapezoid's piecewise-quadratic CDF
+// (projection_common.cuh:139-166).
+//
+// The weights do not depend on the height index h, so every kernel computes
+// them once per (voxel, angle) and applies them to a vector of heights.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace vp {
+
+// Trig used for the per-angle constants.
+//   TRIG_REF:     the hardware approximations (__sincosf, approximate
+//                 reciprocal) that the reference's --use_fast_math build uses
+//                 for cos/sin/sincosf and '/', so results track its kernels.
+//   TRIG_PRECISE: CUDA's accurate sincosf and IEEE division.
+enum TrigMode : int { TRIG_REF = 0, TRIG_PRECISE = 1 };
+
+// Per-angle constants: (c, s) and the CDF parameters (a, b, coeff, cd) with
+// coeff = h/2 and cd = coeff/(b-a) (sp_backward_z0.cuh:45-58).  cd is set to
+// zero when b == a (angles k*pi/2): the quadratic pieces are empty there, and
+// a zero keeps every select in trap_cdf free of inf*0.
+struct AngleConst {
+  float c, s;
+  float a, b, coeff, cd;
+};
+
+__device__ __forceinline__ AngleConst angle_const(float phi, int trig) {
+  AngleConst k;
+  float s, c;
+  if (trig == TRIG_REF) {
+    __sincosf(phi, &s, &c);
+  } else {
+    sincosf(phi, &s, &c);
+  }
+  k.c = c;
+  k.s = s;
+  const float cms = fabsf(0.5f * (c - s));
+  const float cps = fabsf(0.5f * (c + s));
+  const float a = fminf(cms, cps);
+  const float b = fmaxf(cms, cps);
+  const float den = (b - a) + 2.0f * a;
+  float lmax, coeff, cd;
+  if (trig == TRIG_REF) {
+    lmax = __fdividef(1.0f, den);
+    coeff = 0.5f * lmax;
+    cd = (b > a) ? __fdividef(coeff, b - a) : 0.0f;
+  } else {
+    lmax = 1.0f / den;
+    coeff = 0.5f * lmax;
+    cd = (b > a) ? coeff / (b - a) : 0.0f;
+  }
+  k.a = a;
+  k.b = b;
+  k.coeff = coeff;
+  k.cd = cd;
+  return k;
+}
+
+// Trapezoid CDF F(x) for a footprint centred at 0 (projection_common.cuh:139-166):
+//   0                          x <= -b
+//   cd*(x+b)^2                 -b < x < -a
+//   coeff*(b+a) + 2*coeff*x    -a <= x < a
+//   1 - cd*(b-x)^2             a <= x < b
+//   1                          x >= b
+__device__ __forceinline__ float trap_cdf(float x, float a, float b, float coeff, float cd) {
+  const float xl = x + b;
+  const float xr = b - x;
+  const float left = cd * xl * xl;
+  const float mid = coeff * (b + a) + 2.0f * coeff * x;
+  const float right = 1.0f - cd * xr * xr;
+  float r = (x < b) ? right : 1.0f;
+  r = (x < a) ? mid : r;
+  r = (x < -a) ? left : r;
+  r = (x <= -b) ? 0.0f : r;
+  return r;
+}
+
+// Detector coordinate of a voxel with centred coordinates (relx, rely).
+__device__ __forceinline__ float det_coord(float relx, float rely, float c, float s, float pcent) {
+  return relx * c + rely * s + pcent;
+}
+
+// Weights of bins r-1, r, r+1 for a voxel projecting to xp
+// (sp_backward_z0.cuh:84-91): r = round-half-even(xp), xv = r - xp,
+// w0 = F(xv-1/2), w1 = F(xv+1/2) - F(xv-1/2), w2 = 1 - F(xv+1/2).
+struct BinWeights {
+  int r;
+  float w0, w1, w2;
+};
+
+__device__ __forceinline__ BinWeights weights_from_offset(int r, float xv, const AngleConst& k) {
+  BinWeights o;
+  o.r = r;
+  const float v1 = trap_cdf(xv - 0.5f, k.a, k.b, k.coeff, k.cd);
+  const float v2 = trap_cdf(xv + 0.5f, k.a, k.b, k.coeff, k.cd);
+  o.w0 = v1;
+  o.w1 = v2 - v1;
+  o.w2 = 1.0f - v2;
+  return o;
+}
+
+__device__ __forceinline__ BinWeights bin_weights(float xp, const AngleConst& k) {
+  const int r = __float2int_rn(xp);
+  return weights_from_offset(r, (float)r - xp, k);
+}
+
+// Error-free sum: s + e == a + b exactly (Knuth's TwoSum).
+__device__ __forceinline__ float two_sum(float a, float b, float& e) {
+  const float s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+  return s;
+}
+
+// Weights with the sub-bin offset xv = r - xp evaluated from an unrounded xp:
+// the products and sums of xp are carried as (value, error) pairs with FMA
+// and TwoSum, so at 512^3 the offset is not limited by the ~3e-5 px spacing
+// of floats near 256.  Used by TRIG_PRECISE; TRIG_REF keeps the plain formula
+// so that it rounds the way the reference does.
+__device__ __forceinline__ BinWeights bin_weights_compensated(float relx, float rely,
+                                                              const AngleConst& k,
+                                                              float pcent) {
+  const float p1 = __fmul_rn(relx, k.c);
+  const float e1 = fmaf(relx, k.c, -p1);
+  const float p2 = __fmul_rn(rely, k.s);
+  const float e2 = fmaf(rely, k.s, -p2);
+  float e3, e4;
+  const float s1 = two_sum(p1, p2, e3);
+  const float hi = two_sum(s1, pcent, e4);
+  const float lo = (e1 + e2) + (e3 + e4);
+  const int r = __float2int_rn(hi);
+  const float xv = __fsub_rn((float)r, hi) - lo;
+  return weights_from_offset(r, xv, k);
+}
+
+// The weights of voxel (relx, rely) at one angle, in the given trig mode.
+__device__ __forceinline__ BinWeights voxel_weights(float relx, float rely, const AngleConst& k,
+                                                    float pcent, int trig) {
+  if (trig == TRIG_PRECISE) return bin_weights_compensated(relx, rely, k, pcent);
+  return bin_weights(det_coord(relx, rely, k.c, k.s, pcent), k);
+}
+
+__device__ __forceinline__ float4 f4_fma(float w, float4 v, float4 acc) {
+  acc.x = fmaf(w, v.x, acc.x);
+  acc.y = fmaf(w, v.y, acc.y);
+  acc.z = fmaf(w, v.z, acc.z);
+  acc.w = fmaf(w, v.w, acc.w);
+  return acc;
+}
+
+__device__ __forceinline__ float f4_fma(float w, float v, float acc) { return fmaf(w, v, acc); }
+
+__device__ __forceinline__ float4 f4_add(float4 a, float4 b) {
+  return make_float4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w);
+}
+__device__ __forceinline__ float f4_add(float a, float b) { return a + b; }
+
+template <typename T>
+__device__ __forceinline__ T vzero();
+template <>
+__device__ __forceinline__ float vzero<float>() { return 0.0f; }
+template <>
+__device__ __forceinline__ float4 vzero<float4>() { return make_float4(0.f, 0.f, 0.f, 0.f); }
+
+// Geometry shared by all launches.  Volume (SY, SX) comes from x, detector
+// (n_ang, PX) from y; H is min(Hx, Hy): heights past the shorter array read
+// as zero in the reference (border-mode texture) and so leave the output
+// unchanged, which computing only h < H reproduces.
+struct Geom {
+  int SY, SX;       // volume rows / columns
+  int n_ang, PX;    // angles / detector bins
+  int H;            // heights processed
+  int Hx, Hy;       // height extent of x and of y (z_order 0 row strides)
+  float xcent, ycent, pcent;
+  int trig;
+};
+
+}  // namespace vp

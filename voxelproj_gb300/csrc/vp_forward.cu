@@ -1,0 +1,296 @@
+// Forward projection A, detector-driven gather.
+//
+// Replaces the reference kernels sp_forward_z0 (sp_forward_z0.cuh:107-185)
+// and sp_forward_z2 (sp_forward_z2.cuh:102-174).  Those march each ray
+// through a border-mode texture (ray clipped to an extended box,
+// projection_common.cuh:194-272; minor-axis walk, sp_forward_z0.cuh:8-103) and
+// re-evaluate two CDFs per visited voxel for every height.  Here a ray
+// (angle, bin) gathers exactly the voxels whose three-bin footprint reaches
+// it, with the same closed-form weights the adjoint uses, so A and A^T are
+// the same matrix up to float summation order:
+//   weight of bin p from voxel v = w_{p - round(xp_v) + 1}(v)   (bin_weights).
+//
+// Voxel enumeration: along the axis whose unit step moves xp by less
+// ("major"), every index is visited; along the other ("minor", |shift| >=
+// sqrt(1/2)) only the indices whose xp lies within b + 1/2 (+ a small margin)
+// of the bins being gathered.  Voxels the margin admits needlessly get zero
+// weight from the closed form, so the margin only costs time.
+#include <cuda_runtime.h>
+
+#include "vp_common.cuh"
+#include "vp_launch.h"
+
+namespace vp {
+
+namespace {
+
+template <int R>
+struct Vec;
+template <>
+struct Vec<1> {
+  using T = float;
+};
+template <>
+struct Vec<4> {
+  using T = float4;
+};
+
+template <typename V>
+__device__ __forceinline__ V ld_or_zero(const float* p, bool ok) {
+  return ok ? __ldg(reinterpret_cast<const V*>(p)) : vzero<V>();
+}
+
+constexpr float kWindowMargin = 1e-3f;
+
+// Minor-axis index range [lo, hi] (clamped to [0, n_minor)) of voxels on major
+// line i whose detector coordinate can fall in [t_lo, t_hi].
+struct MinorRange {
+  int lo, hi;
+};
+
+__device__ __forceinline__ MinorRange minor_range(int i, float cent_major, float sh_major,
+                                                  float cent_minor, float inv_sh_minor,
+                                                  int n_minor, float pcent, float t_lo,
+                                                  float t_hi) {
+  const float K = ((float)i - cent_major) * sh_major + pcent;
+  const float u1 = (t_lo - K) * inv_sh_minor + cent_minor;
+  const float u2 = (t_hi - K) * inv_sh_minor + cent_minor;
+  MinorRange m;
+  m.lo = max(0, (int)ceilf(fminf(u1, u2)));
+  m.hi = min(n_minor - 1, (int)floorf(fmaxf(u1, u2)));
+  return m;
+}
+
+// ---------------------------------------------------------------------------
+// z_order 0: x (SY, SX, H), y (n_ang, PX, H); heights contiguous.
+// A warp owns angle a, FP0_KW consecutive bins and 32*R heights (lane <->
+// heights).  The voxels gathered are warp-uniform, so the warp enumerates
+// them cooperatively: lane j takes major line i0+j, computes its candidate
+// voxels and their bin weights into a per-warp shared list (offsets from a
+// warp prefix sum), then all lanes stream the list with broadcast reads and
+// accumulate the FP0_KW bins in registers.  A candidate's three bins sit at
+// run-relative offsets q-2, q-1, q (q = round(xp) - p0 + 1), dispatched with
+// a warp-uniform switch.
+// ---------------------------------------------------------------------------
+constexpr int FP0_KW = 4;
+constexpr int FP0_WARPS = 4;
+constexpr int FP0_CAP = 10;  // >= max candidates per major line: (KW + 2b)/sqrt(1/2) + 1
+
+static_assert(FP0_KW == 4, "the dispatch switch below lists q = 0..KW+1");
+
+// Adds a candidate's weights to the run's accumulators: bin q-2 gets w0, q-1
+// gets w1, q gets w2 (run-relative); bins outside [0, KW) are dropped.
+template <int KW, int Q, typename V>
+__device__ __forceinline__ void scatter3(V (&acc)[KW], const float4& e, const V& xv) {
+  if constexpr (Q - 2 >= 0 && Q - 2 < KW) acc[Q - 2] = f4_fma(e.x, xv, acc[Q - 2]);
+  if constexpr (Q - 1 >= 0 && Q - 1 < KW) acc[Q - 1] = f4_fma(e.y, xv, acc[Q - 1]);
+  if constexpr (Q < KW) acc[Q] = f4_fma(e.z, xv, acc[Q]);
+}
+
+template <int R>
+__global__ void __launch_bounds__(32 * FP0_WARPS)
+    fp_z0_kernel(const float* __restrict__ x, float* __restrict__ y,
+                 const float* __restrict__ angles, Geom g, int a_base) {
+  using V = typename Vec<R>::T;
+  __shared__ float4 cand[FP0_WARPS][32 * FP0_CAP];
+
+  const int lane = threadIdx.x;
+  const int w = threadIdx.y;
+  const int h = (blockIdx.x * 32 + lane) * R;
+  const int p0 = (blockIdx.y * FP0_WARPS + w) * FP0_KW;
+  const int a = a_base + blockIdx.z;
+  if (p0 >= g.PX || a >= g.n_ang) return;  // warp-uniform
+  const bool hv = h < g.H;
+
+  const AngleConst k = angle_const(__ldg(angles + a), g.trig);
+  const bool minor_x = fabsf(k.c) >= fabsf(k.s);
+  const int n_major = minor_x ? g.SY : g.SX;
+  const int n_minor = minor_x ? g.SX : g.SY;
+  const float cent_major = minor_x ? g.ycent : g.xcent;
+  const float cent_minor = minor_x ? g.xcent : g.ycent;
+  const float sh_major = minor_x ? k.s : k.c;
+  const float inv_sh_minor = 1.0f / (minor_x ? k.c : k.s);
+  const float t_lo = (float)p0 - 0.5f - k.b - kWindowMargin;
+  const float t_hi = (float)(p0 + FP0_KW) - 0.5f + k.b + kWindowMargin;
+
+  V acc[FP0_KW];
+#pragma unroll
+  for (int b = 0; b < FP0_KW; ++b) acc[b] = vzero<V>();
+
+  for (int i0 = 0; i0 < n_major; i0 += 32) {
+    const int i = i0 + lane;
+    int lo = 0, cnt = 0;
+    if (i < n_major) {
+      const MinorRange mr = minor_range(i, cent_major, sh_major, cent_minor, inv_sh_minor,
+                                        n_minor, g.pcent, t_lo, t_hi);
+      lo = mr.lo;
+      cnt = max(0, min(mr.hi - mr.lo + 1, FP0_CAP));
+    }
+    int incl = cnt;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const int n = __shfl_up_sync(0xffffffffu, incl, d);
+      if (lane >= d) incl += n;
+    }
+    const int total = __shfl_sync(0xffffffffu, incl, 31);
+    const int start = incl - cnt;
+    for (int t = 0; t < cnt; ++t) {
+      const int m = lo + t;
+      const int xi = minor_x ? m : i;
+      const int yi = minor_x ? i : m;
+      const BinWeights bw =
+          voxel_weights((float)xi - g.xcent, (float)yi - g.ycent, k, g.pcent, g.trig);
+      int q = bw.r - p0 + 1;
+      float4 e = make_float4(bw.w0, bw.w1, bw.w2, 0.0f);
+      if (q < 0 || q > FP0_KW + 1) {
+        q = 0;
+        e = make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+      const int vox = yi * g.SX + xi;
+      e.w = __int_as_float((vox << 3) | q);
+      cand[w][start + t] = e;
+    }
+    __syncwarp();
+    for (int c = 0; c < total; ++c) {
+      const float4 e = cand[w][c];
+      const int pk = __float_as_int(e.w);
+      const int vox = pk >> 3;
+      const int q = pk & 7;
+      const V xv = ld_or_zero<V>(x + (size_t)vox * g.Hx + h, hv);
+      switch (q) {
+        case 0: scatter3<FP0_KW, 0>(acc, e, xv); break;
+        case 1: scatter3<FP0_KW, 1>(acc, e, xv); break;
+        case 2: scatter3<FP0_KW, 2>(acc, e, xv); break;
+        case 3: scatter3<FP0_KW, 3>(acc, e, xv); break;
+        case 4: scatter3<FP0_KW, 4>(acc, e, xv); break;
+        default: scatter3<FP0_KW, 5>(acc, e, xv); break;
+      }
+    }
+    __syncwarp();
+  }
+
+  if (hv) {
+#pragma unroll
+    for (int b = 0; b < FP0_KW; ++b) {
+      const int p = p0 + b;
+      if (p < g.PX) {
+        V* py = reinterpret_cast<V*>(y + ((size_t)a * g.PX + p) * g.Hy + h);
+        *py = f4_add(*py, acc[b]);
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// z_order 2: x (H, SY, SX), y (H, n_ang, PX); SX / PX contiguous.
+// A thread owns one bin p (lane <-> p, so the output row is coalesced) of one
+// angle and FP2_RH heights, walks the major axis, and gathers the candidate
+// voxels of its bin; each weight is reused across the thread's heights.
+// ---------------------------------------------------------------------------
+constexpr int FP2_RH = 8;
+constexpr int FP2_WARPS = 4;
+
+__global__ void __launch_bounds__(32 * FP2_WARPS)
+    fp_z2_kernel(const float* __restrict__ x, float* __restrict__ y,
+                 const float* __restrict__ angles, Geom g, int a_base) {
+  const int lane = threadIdx.x;
+  const int w = threadIdx.y;
+  const int p = blockIdx.x * 32 + lane;
+  const int a = a_base + blockIdx.y * FP2_WARPS + w;
+  const int h0 = blockIdx.z * FP2_RH;
+  if (a >= g.n_ang) return;  // warp-uniform
+  const bool pv = p < g.PX;
+
+  const AngleConst k = angle_const(__ldg(angles + a), g.trig);
+  const bool minor_x = fabsf(k.c) >= fabsf(k.s);
+  const int n_major = minor_x ? g.SY : g.SX;
+  const int n_minor = minor_x ? g.SX : g.SY;
+  const float cent_major = minor_x ? g.ycent : g.xcent;
+  const float cent_minor = minor_x ? g.xcent : g.ycent;
+  const float sh_major = minor_x ? k.s : k.c;
+  const float inv_sh_minor = 1.0f / (minor_x ? k.c : k.s);
+  const float t_lo = (float)p - 0.5f - k.b - kWindowMargin;
+  const float t_hi = (float)p + 0.5f + k.b + kWindowMargin;
+  const size_t xh_stride = (size_t)g.SY * g.SX;
+
+  float acc[FP2_RH];
+#pragma unroll
+  for (int i = 0; i < FP2_RH; ++i) acc[i] = 0.0f;
+
+  if (pv) {
+    for (int i = 0; i < n_major; ++i) {
+      const MinorRange mr = minor_range(i, cent_major, sh_major, cent_minor, inv_sh_minor,
+                                        n_minor, g.pcent, t_lo, t_hi);
+      for (int m = mr.lo; m <= mr.hi; ++m) {
+        const int xi = minor_x ? m : i;
+        const int yi = minor_x ? i : m;
+        const BinWeights bw =
+            voxel_weights((float)xi - g.xcent, (float)yi - g.ycent, k, g.pcent, g.trig);
+        const int q = p - bw.r + 1;
+        const float wt = (q == 0) ? bw.w0 : (q == 1) ? bw.w1 : (q == 2) ? bw.w2 : 0.0f;
+        if (wt != 0.0f) {
+          const float* px = x + (size_t)yi * g.SX + xi;
+#pragma unroll
+          for (int r = 0; r < FP2_RH; ++r) {
+            const int h = h0 + r;
+            if (h < g.H) acc[r] = fmaf(wt, __ldg(px + (size_t)h * xh_stride), acc[r]);
+          }
+        }
+      }
+    }
+    const size_t yh_stride = (size_t)g.n_ang * g.PX;
+#pragma unroll
+    for (int r = 0; r < FP2_RH; ++r) {
+      const int h = h0 + r;
+      if (h < g.H) y[(size_t)h * yh_stride + (size_t)a * g.PX + p] += acc[r];
+    }
+  }
+}
+
+inline unsigned ceil_div(long long a, long long b) { return (unsigned)((a + b - 1) / b); }
+constexpr int kMaxGridYZ = 65535;
+
+}  // namespace
+
+int launches_forward_z0(const Geom& g) {
+  return (int)ceil_div(g.n_ang, kMaxGridYZ);
+}
+
+int launches_forward_z2(const Geom& g) {
+  return (int)ceil_div(g.n_ang, (long long)kMaxGridYZ * FP2_WARPS);
+}
+
+cudaError_t launch_forward_z0(const float* x, float* y, const float* angles, const Geom& g,
+                              cudaStream_t stream) {
+  const bool vec4 = (g.Hx % 4 == 0) && (g.Hy % 4 == 0) &&
+                    ((reinterpret_cast<uintptr_t>(x) | reinterpret_cast<uintptr_t>(y)) & 15) == 0;
+  const int R = vec4 ? 4 : 1;
+  dim3 block(32, FP0_WARPS);
+  for (int a_base = 0; a_base < g.n_ang; a_base += kMaxGridYZ) {
+    const int na = g.n_ang - a_base < kMaxGridYZ ? g.n_ang - a_base : kMaxGridYZ;
+    dim3 grid(ceil_div(g.H, 32 * R), ceil_div(g.PX, FP0_KW * FP0_WARPS), na);
+    if (vec4)
+      fp_z0_kernel<4><<<grid, block, 0, stream>>>(x, y, angles, g, a_base);
+    else
+      fp_z0_kernel<1><<<grid, block, 0, stream>>>(x, y, angles, g, a_base);
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+cudaError_t launch_forward_z2(const float* x, float* y, const float* angles, const Geom& g,
+                              cudaStream_t stream) {
+  dim3 block(32, FP2_WARPS);
+  const long long per_launch = (long long)kMaxGridYZ * FP2_WARPS;
+  for (long long a_base = 0; a_base < g.n_ang; a_base += per_launch) {
+    const long long na = g.n_ang - a_base < per_launch ? g.n_ang - a_base : per_launch;
+    dim3 grid(ceil_div(g.PX, 32), ceil_div(na, FP2_WARPS), ceil_div(g.H, FP2_RH));
+    fp_z2_kernel<<<grid, block, 0, stream>>>(x, y, angles, g, (int)a_base);
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+}  // namespace vp

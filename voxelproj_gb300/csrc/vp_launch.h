@@ -1,0 +1,28 @@
+// Internal launch interface between the C-ABI layer (vp_capi.cu) and the
+// kernel translation units.  Every launcher enqueues on `stream`, never
+// synchronises, and returns the launch status.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "vp_common.cuh"
+
+namespace vp {
+
+// y (z_order 0: (n_ang, PX, Hy), z_order 2: (Hy, n_ang, PX)) += A x.
+cudaError_t launch_forward_z0(const float* x, float* y, const float* angles, const Geom& g,
+                              cudaStream_t stream);
+cudaError_t launch_forward_z2(const float* x, float* y, const float* angles, const Geom& g,
+                              cudaStream_t stream);
+// x (z_order 0: (SY, SX, Hx), z_order 2: (Hx, SY, SX)) += A^T y.
+cudaError_t launch_backward_z0(const float* y, float* x, const float* angles, const Geom& g,
+                               cudaStream_t stream);
+cudaError_t launch_backward_z2(const float* y, float* x, const float* angles, const Geom& g,
+                               cudaStream_t stream);
+
+// Kernel launches the forward launchers issue for a geometry (grids are
+// split past 65535 angle blocks).
+int launches_forward_z0(const Geom& g);
+int launches_forward_z2(const Geom& g);
+
+}  // namespace vp

@@ -1,0 +1,120 @@
+"""Drop-in Python API: ``forward`` (A) and ``backward`` (A^T).
+
+Mirrors voxelproj/wrappers.py:10-122 of the reference:
+
+* ``x``/``y`` may be numpy arrays, CPU tensors or CUDA tensors of any dtype;
+  they are moved to CUDA as float32.
+* The output argument may be ``None`` (default shape), a shape tuple, or a
+  container.  A container is ACCUMULATED into (``out += result``) and is the
+  object returned (same ``id``); numpy containers are filled with
+  ``np.copyto``, tensors with ``copy_`` unless the CUDA float32 tensor itself
+  was computed into.
+* Without a container the result comes back in the input's kind: numpy in,
+  numpy out; tensor in, tensor on the input's device.
+* Default output shapes (wrappers.py:40-43, :88-91):
+  forward z0 (n_ang, max(SY,SX), H), z2 (H, n_ang, max(SY,SX));
+  backward z0 (PX, PX, H), z2 (H, PX, PX).
+* ``z_order`` other than 0 or 2 raises ``KeyError`` (dict dispatch, :44-47).
+* ``block_size`` is accepted for compatibility and ignored.
+
+Beyond the reference: ``angles`` may also be a list or tuple (the reference
+accepted only arrays/tensors), non-contiguous inputs and outputs are handled
+instead of rejected or mis-written, and there is no 512-angle limit.
+"""
+
+from __future__ import annotations
+
+import numpy as np
+import torch
+
+from ._CU import backward_z0, backward_z2, forward_z0, forward_z2
+
+
+def gpu_array_with_default_shape(x=None, shape=None):
+    """None or a shape tuple -> zeros on CUDA; array/tensor -> float32 CUDA
+    tensor (no copy when it already is one).  As wrappers.py:10-25."""
+    if x is None:
+        return torch.zeros(shape, dtype=torch.float32, device="cuda")
+    if isinstance(x, tuple):
+        return torch.zeros(x, dtype=torch.float32, device="cuda")
+    if isinstance(x, np.ndarray):
+        return torch.tensor(x, dtype=torch.float32, device="cuda")
+    if isinstance(x, torch.Tensor):
+        return x.to(dtype=torch.float32, device="cuda")
+    raise TypeError("x must be None, a shape tuple, or an array/tensor")
+
+
+def _angles_gpu(angles) -> torch.Tensor:
+    if isinstance(angles, (list, tuple)):
+        angles = np.asarray(angles, dtype=np.float32)
+    a = gpu_array_with_default_shape(angles)
+    return a.reshape(-1).contiguous()
+
+
+def _input_gpu(v) -> torch.Tensor:
+    return gpu_array_with_default_shape(v).contiguous()
+
+
+def _finish(out, out_gpu, work, src_kind, src_device):
+    """Copies back into a caller's container or returns a new array in the
+    input's kind (wrappers.py:57-73)."""
+    if work is not out_gpu:
+        out_gpu.copy_(work)
+    if isinstance(out, np.ndarray):
+        if out.dtype == np.float32 and out.flags.c_contiguous and out.flags.writeable:
+            torch.from_numpy(out).copy_(out_gpu)  # one device-to-host copy
+        else:
+            np.copyto(out, out_gpu.cpu().numpy())
+        return out
+    if isinstance(out, torch.Tensor):
+        if out.data_ptr() != out_gpu.data_ptr() or out.device != out_gpu.device:
+            out.copy_(out_gpu)
+        return out
+    if src_kind == "numpy":
+        return out_gpu.cpu().numpy()
+    return out_gpu.to(src_device) if src_device is not None else out_gpu
+
+
+def _kind(v):
+    if isinstance(v, np.ndarray):
+        return "numpy", None
+    if isinstance(v, torch.Tensor) and not v.is_cuda:
+        return "tensor", v.device
+    return "cuda", None
+
+
+def forward(x, angles, y, z_order=0, block_size=[8, 8, 8]):
+    """Forward projection: returns y + A x (see module docstring)."""
+    kind, device = _kind(x)
+    n_ang = len(angles)
+    default_shape = {
+        0: (n_ang, max(x.shape[0], x.shape[1]), x.shape[2]),
+        2: (x.shape[0], n_ang, max(x.shape[1], x.shape[2])),
+    }
+    project = {0: forward_z0, 2: forward_z2}
+    shape = default_shape[z_order]
+    fn = project[z_order]
+    x_gpu = _input_gpu(x)
+    a_gpu = _angles_gpu(angles)
+    y_gpu = gpu_array_with_default_shape(y, shape=shape)
+    work = y_gpu if y_gpu.is_contiguous() else y_gpu.contiguous()
+    fn(x_gpu, work, a_gpu, block_size=block_size)
+    return _finish(y, y_gpu, work, kind, device)
+
+
+def backward(y, angles, x, z_order=0, block_size=[8, 8, 8]):
+    """Backprojection: returns x + A^T y (see module docstring)."""
+    kind, device = _kind(y)
+    default_shape = {
+        0: (y.shape[1], y.shape[1], y.shape[2]),
+        2: (y.shape[0], y.shape[2], y.shape[2]),
+    }
+    project = {0: backward_z0, 2: backward_z2}
+    shape = default_shape[z_order]
+    fn = project[z_order]
+    y_gpu = _input_gpu(y)
+    a_gpu = _angles_gpu(angles)
+    x_gpu = gpu_array_with_default_shape(x, shape=shape)
+    work = x_gpu if x_gpu.is_contiguous() else x_gpu.contiguous()
+    fn(y_gpu, work, a_gpu, block_size=block_size)
+    return _finish(x, x_gpu, work, kind, device)

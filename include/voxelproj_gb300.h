@@ -39,6 +39,7 @@
 #ifndef VOXELPROJ_GB300_H
 #define VOXELPROJ_GB300_H
 
+#include <stddef.h>
 #include <stdint.h>
 
 #if defined(__GNUC__)
@@ -59,6 +60,7 @@ extern "C" {
 #define VP_ERR_CUDA 4           /* a CUDA runtime call failed; see vp_last_cuda_error() */
 #define VP_ERR_BAD_FLAGS 5      /* unknown bit in `flags` */
 #define VP_ERR_BAD_Z_ORDER 6    /* z_order other than 0 or 2 */
+#define VP_ERR_WORKSPACE 7      /* workspace smaller than vp_z2_workspace_bytes() */
 
 /* Flags. */
 #define VP_FLAG_TRIG_PRECISE 1  /* accurate sincosf / IEEE division for the per-angle
@@ -78,6 +80,14 @@ VP_API int vp_last_cuda_error(void);
  * No counterpart in the reference; lets callers and benchmarks see how many
  * GPU launches a sequence of calls issued. */
 VP_API uint64_t vp_launch_count(void);
+
+/* Kernel variant selection, used by the autotuner and for measurements.
+ * op: 0 = forward z0, 1 = backward z0, 2 = forward z2, 3 = backward z2;
+ * variant 0 = automatic (default).  Unknown variants fall back to automatic.
+ * Process-wide; no counterpart in the reference (its only tuning knob,
+ * block_size, is accepted and ignored by the Python layer). */
+VP_API int vp_set_kernel_variant(int op, int variant);
+VP_API int vp_get_kernel_variant(int op);
 
 /* y += A x, z_order 0.  x (x0=SY, x1=SX, x2=Hx), y (y0=n_ang, y1=PX, y2=Hy).
  * Replaces voxelproj._CU.forward_z0 (voxelproj/csrc/projectors.cu:34-104). */
@@ -102,6 +112,25 @@ VP_API int vp_forward_z2(const float* x, int64_t x0, int64_t x1, int64_t x2,
 VP_API int vp_backward_z2(const float* y, int64_t y0, int64_t y1, int64_t y2,
                    float* x, int64_t x0, int64_t x1, int64_t x2,
                    const float* angles, int64_t n_angles, int flags, void* stream);
+
+/* z_order 2 with caller-supplied scratch.  For H >= 32 the z_order 2
+ * operators transpose to height-fastest order, run the z_order 0 kernels and
+ * transpose back (adding into the output); they need
+ * vp_z2_workspace_bytes(...) bytes of device scratch (0 when H < 32).  The
+ * plain vp_forward_z2 / vp_backward_z2 take it from a library-private
+ * stream-ordered pool; these variants use `workspace` instead and fail with
+ * VP_ERR_WORKSPACE if it is too small.  No counterpart in the reference,
+ * which staged its input through a per-call cudaArray. */
+VP_API size_t vp_z2_workspace_bytes(int64_t x0, int64_t x1, int64_t x2,
+                                    int64_t y0, int64_t y1, int64_t y2);
+VP_API int vp_forward_z2_ws(const float* x, int64_t x0, int64_t x1, int64_t x2,
+                            float* y, int64_t y0, int64_t y1, int64_t y2,
+                            const float* angles, int64_t n_angles, int flags,
+                            void* workspace, size_t workspace_bytes, void* stream);
+VP_API int vp_backward_z2_ws(const float* y, int64_t y0, int64_t y1, int64_t y2,
+                             float* x, int64_t x0, int64_t x1, int64_t x2,
+                             const float* angles, int64_t n_angles, int flags,
+                             void* workspace, size_t workspace_bytes, void* stream);
 
 /* z_order dispatch, as voxelproj.wrappers.forward/backward select a kernel by
  * z_order (voxelproj/wrappers.py:44-47, :92-95); dims as for the

@@ -1,4 +1,4 @@
-"""TEST INFRASTRUCTURE ONLY — builds the reference's own CUDA kernels as a checker.
+"""TEST INFRASTRUCTURE ONLY — builds the reference's own CUDA kernels for golden fixtures.
 
 Compiles the reference voxelproj extension (``voxelproj._CU``: the files
 ``voxelproj.cpp`` and ``projectors.cu`` with their ``include/*.cuh``) from the

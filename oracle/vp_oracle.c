@@ -1,8 +1,8 @@
 /*
  * TEST INFRASTRUCTURE ONLY — the oracle.  Nothing in the voxelproj_gb300
  * package loads or calls this file; only tests/, __graft_entry__.smoke() and
- * bench.py's CPU-baseline leg do, as the checker or as the timed CPU
- * baseline.
+ * bench.py's CPU-baseline leg do, as the reference for parity or as the
+ * timed CPU baseline.
  *
  * CPU restatement of the reference voxelproj exact-trapezoid projector pair,
  * written from its mathematics:

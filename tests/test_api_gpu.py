@@ -108,7 +108,7 @@ def test_adjointness(z, px):
     rhs = np.vdot(x.astype(np.float64), ATy.astype(np.float64))
     np.testing.assert_allclose(lhs, rhs, rtol=1e-3, atol=1e-4)  # the reference's bound
     den = np.linalg.norm(Ax) * np.linalg.norm(y)
-    assert abs(lhs - rhs) / den <= tol.ADJOINT  # the benchmark spec's bound
+    assert abs(lhs - rhs) / den <= tol.ADJOINT  # the parity target's bound
 
 
 # ---- beyond the reference's tests ----------------------------------------

@@ -60,11 +60,13 @@ def oracle_outputs(c):
     return fwd, bwd
 
 
-# The reference's forward marches rays with an accumulated float position
-# (sp_forward_z0.cuh:33,53) and both directions use hardware sin/cos, so the
-# reference itself is some 1e-6..1e-5 away from the exact operator at these
-# sizes; the oracle must agree to that level.
-ORACLE_VS_REFERENCE = 5e-5
+# How far the reference itself is from the exact operator at these sizes
+# (fixtures up to 68 voxels wide; angles up to 4*pi in rand_angles):
+#   A^T: closed-form 3-bin weights, but hardware sin/cos  -> ~1e-5
+#   A:   rays marched with an accumulated float position
+#        (sp_forward_z0.cuh:33,53) and clipped in float   -> ~1e-4
+#        (it reaches 5.9e-3 at 512^3, measured on a GB300)
+ORACLE_VS_REFERENCE = {"A": 1.5e-4, "AT": 2e-5}
 
 
 @pytest.mark.parametrize("name", NAMES)
@@ -74,12 +76,16 @@ def test_oracle_matches_reference(name):
     ef = rel_err(c["fwd"] - c["y0"], fwd - c["y0"])
     eb = rel_err(c["bwd"] - c["x0"], bwd - c["x0"])
     print(f"\n[oracle vs reference] {name}: A {ef:.3e}  A^T {eb:.3e}")
-    assert ef <= ORACLE_VS_REFERENCE and eb <= ORACLE_VS_REFERENCE
+    assert ef <= ORACLE_VS_REFERENCE["A"] and eb <= ORACLE_VS_REFERENCE["AT"]
 
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("name", NAMES)
 def test_kernels_match_reference(name):
+    """A^T: within the parity target (1e-5) of the reference's kernels.
+    A: the reference's forward carries its own ray-march error, so the bound
+    is: our distance to the reference is no more than the reference's
+    distance to the FP64 operator plus our own (REF_VS_FP64)."""
     import voxelproj_gb300 as vp
 
     c = CASES[name]
@@ -91,7 +97,16 @@ def test_kernels_match_reference(name):
     xo = torch.tensor(c["x0"], device=dev)
     (vp._CU.backward_z0 if z == 0 else vp._CU.backward_z2)(torch.tensor(c["y"], device=dev), xo, a)
     torch.cuda.synchronize()
-    ef = rel_err(yo.cpu().numpy() - c["y0"], c["fwd"] - c["y0"])
+    fwd64, _ = oracle_outputs(c)
+    got_a = yo.cpu().numpy() - c["y0"]
+    ref_a = c["fwd"] - c["y0"]
+    exact_a = fwd64 - c["y0"]
+    e_ref = rel_err(got_a, ref_a)
+    e_ours64 = rel_err(got_a, exact_a)
+    e_ref64 = rel_err(ref_a, exact_a)
     eb = rel_err(xo.cpu().numpy() - c["x0"], c["bwd"] - c["x0"])
-    print(f"\n[kernels vs reference] {name}: A {ef:.3e}  A^T {eb:.3e}")
-    assert ef <= tol.REF_VS_REFERENCE and eb <= tol.REF_VS_REFERENCE
+    print(f"\n[kernels vs reference] {name}: A {e_ref:.3e} (ours vs FP64 {e_ours64:.3e}, "
+          f"reference vs FP64 {e_ref64:.3e})  A^T {eb:.3e}")
+    assert eb <= tol.REF_VS_REFERENCE
+    assert e_ours64 <= tol.REF_VS_FP64
+    assert e_ref <= e_ref64 + tol.REF_VS_FP64

@@ -85,7 +85,8 @@ def test_matches_fp64_oracle(geom, z, trig):
     ATy = oracle.backward(y, ang, SY, SX, z)
     ef = rel_err(got_f - y0, Ax)
     eb = rel_err(got_b - x0, ATy)
-    bound = tol.PRECISE_VS_FP64 if trig == "precise" else tol.REF_VS_FP64
+    n_ext = max(SY, SX, PX)
+    bound = tol.precise_vs_fp64(n_ext) if trig == "precise" else tol.ref_vs_fp64(n_ext)
     print(f"\n[parity] z={z} {trig:9s} {geom}: A {ef:.3e}  A^T {eb:.3e}")
     assert ef <= bound and eb <= bound, (ef, eb)
     # accumulate semantics: the initial content is kept, not overwritten

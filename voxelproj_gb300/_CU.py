@@ -74,11 +74,22 @@ def _call(fn_name: str, inp, out, angles) -> None:
     _check_other(angles, "angles", inp.device, None)
     if out.data_ptr() == inp.data_ptr() and inp.numel() > 0:
         raise RuntimeError("in and out must not alias")
-    fn = getattr(_lib.LIB, fn_name)
     with torch.cuda.device(inp.device):
         stream = torch.cuda.current_stream(inp.device).cuda_stream
-        status = fn(inp.data_ptr(), *inp.shape, out.data_ptr(), *out.shape, angles.data_ptr(),
-                    angles.numel(), _flags, stream)
+        if fn_name.endswith("z2"):
+            # scratch for the transposed path, from torch's caching allocator
+            x, y = (inp, out) if fn_name.startswith("vp_forward") else (out, inp)
+            nbytes = _lib.LIB.vp_z2_workspace_bytes(*x.shape, *y.shape)
+            ws = torch.empty((nbytes + 3) // 4, dtype=torch.float32, device=inp.device) \
+                if nbytes else None
+            fn = getattr(_lib.LIB, fn_name + "_ws")
+            status = fn(inp.data_ptr(), *inp.shape, out.data_ptr(), *out.shape,
+                        angles.data_ptr(), angles.numel(), _flags,
+                        ws.data_ptr() if ws is not None else None, nbytes, stream)
+        else:
+            fn = getattr(_lib.LIB, fn_name)
+            status = fn(inp.data_ptr(), *inp.shape, out.data_ptr(), *out.shape,
+                        angles.data_ptr(), angles.numel(), _flags, stream)
     _lib.check(status, fn_name[3:])
 
 

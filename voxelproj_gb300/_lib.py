@@ -19,6 +19,7 @@ VP_ERR_ANGLES = 3
 VP_ERR_CUDA = 4
 VP_ERR_BAD_FLAGS = 5
 VP_ERR_BAD_Z_ORDER = 6
+VP_ERR_WORKSPACE = 7
 
 VP_FLAG_TRIG_PRECISE = 1
 
@@ -32,10 +33,17 @@ SIGNATURES = {
     "vp_error_string": (ctypes.c_char_p, [_I]),
     "vp_last_cuda_error": (_I, []),
     "vp_launch_count": (ctypes.c_uint64, []),
+    "vp_set_kernel_variant": (_I, [_I, _I]),
+    "vp_get_kernel_variant": (_I, [_I]),
     "vp_forward_z0": (_I, [_P, _I64, _I64, _I64, _P, _I64, _I64, _I64, _P, _I64, _I, _P]),
     "vp_backward_z0": (_I, [_P, _I64, _I64, _I64, _P, _I64, _I64, _I64, _P, _I64, _I, _P]),
     "vp_forward_z2": (_I, [_P, _I64, _I64, _I64, _P, _I64, _I64, _I64, _P, _I64, _I, _P]),
     "vp_backward_z2": (_I, [_P, _I64, _I64, _I64, _P, _I64, _I64, _I64, _P, _I64, _I, _P]),
+    "vp_z2_workspace_bytes": (ctypes.c_size_t, [_I64, _I64, _I64, _I64, _I64, _I64]),
+    "vp_forward_z2_ws": (_I, [_P, _I64, _I64, _I64, _P, _I64, _I64, _I64, _P, _I64, _I, _P,
+                              ctypes.c_size_t, _P]),
+    "vp_backward_z2_ws": (_I, [_P, _I64, _I64, _I64, _P, _I64, _I64, _I64, _P, _I64, _I, _P,
+                               ctypes.c_size_t, _P]),
     "vp_forward": (_I, [_P, _P, _P, _P, _P, _I64, _I, _I, _P]),
     "vp_backward": (_I, [_P, _P, _P, _P, _P, _I64, _I, _I, _P]),
 }

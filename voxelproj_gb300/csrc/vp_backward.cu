@@ -109,7 +109,135 @@ __global__ void __launch_bounds__(32 * BP0_WARPS)
       const int xi = xi0 + m;
       if (xi < g.SX) {
         V* px = reinterpret_cast<V*>(x + ((size_t)yi * g.SX + xi) * g.Hx + h);
-        *px = f4_add(*px, acc[m]);
+        store_out(px, acc[m], g.accumulate);
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// z_order 0, register-blocked: a warp owns a BX x BY block of voxel columns
+// and 128 heights (lane <-> 4 heights, float4).  At one angle the block's
+// voxels land on bins [base, base + W) with W <= 3 + floor(dmax + 1), where
+// dmax = sqrt((BX-1)^2 + (BY-1)^2) bounds the spread of xp over the block and
+// the +1 covers rounding.  That window is loaded once into registers (about
+// 7 float4 loads for 16 voxels instead of 48), and each voxel reads its
+// three bins from it through a warp-uniform switch on its window offset
+// o = round(xp) - base - 1, so every register index stays static.
+//
+// Per (voxel, angle) the lane-parallel table phase stores (w0, w1, w2, r);
+// per angle it stores (rmin, W).
+// ---------------------------------------------------------------------------
+constexpr int BPB_WARPS = 4;
+constexpr int BPB_CHUNK = 32;
+
+constexpr int isqrt(int v) {
+  int r = 0;
+  while ((r + 1) * (r + 1) <= v) ++r;
+  return r;
+}
+
+template <int BX, int BY>
+struct BlockWindow {
+  // |xp_i - xp_j| <= sqrt((BX-1)^2 + (BY-1)^2) over the block (Cauchy-Schwarz)
+  // and |round(xp) - xp| <= 1/2, so round(xp) spans at most
+  // floor(sqrt(D2) + 1) = isqrt(D2) + 1.
+  static constexpr int D2 = (BX - 1) * (BX - 1) + (BY - 1) * (BY - 1);
+  static constexpr int OMAX = isqrt(D2) + 1;  // largest window offset of a voxel
+  static constexpr int WMAX = OMAX + 3;       // largest window
+};
+
+// acc += e.x * win[O] + e.y * win[O+1] + e.z * win[O+2] for the runtime offset
+// held in e.w; the cases are generated up to OMAX.
+template <int O, int OMAX, typename V>
+__device__ __forceinline__ void apply_window(V& acc, const float4& e, const V* win, int o) {
+  if constexpr (O <= OMAX) {
+    if (o == O) {
+      acc = f4_fma(e.x, win[O], acc);
+      acc = f4_fma(e.y, win[O + 1], acc);
+      acc = f4_fma(e.z, win[O + 2], acc);
+    } else {
+      apply_window<O + 1, OMAX>(acc, e, win, o);
+    }
+  }
+}
+
+template <int BX, int BY>
+__global__ void __launch_bounds__(32 * BPB_WARPS)
+    bp_z0_block_kernel(const float* __restrict__ y, float* __restrict__ x,
+                       const float* __restrict__ angles, Geom g, int nbx, int nblocks) {
+  using V = float4;
+  using BW = BlockWindow<BX, BY>;
+  constexpr int NV = BX * BY;
+  constexpr int OMAX = BW::OMAX;
+  constexpr int WMAX = BW::WMAX;
+  __shared__ float4 tw[BPB_WARPS][BPB_CHUNK][NV];
+  __shared__ int2 tb[BPB_WARPS][BPB_CHUNK];
+
+  const int lane = threadIdx.x;
+  const int w = threadIdx.y;
+  const int h = (blockIdx.x * 32 + lane) * 4;
+  const int bidx = blockIdx.y * BPB_WARPS + w;
+  if (bidx >= nblocks) return;  // warp-uniform; tables are per warp
+  const int xi0 = (bidx % nbx) * BX;
+  const int yi0 = (bidx / nbx) * BY;
+  const bool hv = h < g.H;
+
+  V acc[NV];
+#pragma unroll
+  for (int v = 0; v < NV; ++v) acc[v] = vzero<V>();
+
+  const size_t yrow_stride = (size_t)g.PX * g.Hy;
+
+  for (int a0 = 0; a0 < g.n_ang; a0 += BPB_CHUNK) {
+    const int a = a0 + lane;
+    if (a < g.n_ang) {
+      const AngleConst k = angle_const(angles[a], g.trig);
+      int rmin = 0x7fffffff, rmax = -0x7fffffff;
+#pragma unroll
+      for (int v = 0; v < NV; ++v) {
+        const float relx = (float)(xi0 + v % BX) - g.xcent;
+        const float rely = (float)(yi0 + v / BX) - g.ycent;
+        const BinWeights bw = voxel_weights(relx, rely, k, g.pcent, g.trig);
+        rmin = min(rmin, bw.r);
+        rmax = max(rmax, bw.r);
+        tw[w][lane][v] = make_float4(bw.w0, bw.w1, bw.w2, __int_as_float(bw.r));
+      }
+      // window [rmin - 1, rmin - 1 + W); a voxel's offset in it is r - rmin
+      tb[w][lane] = make_int2(rmin, min(rmax - rmin + 3, WMAX));
+    }
+    __syncwarp();
+    const int na = min(BPB_CHUNK, g.n_ang - a0);
+    const float* yang = y + (size_t)a0 * yrow_stride + h;
+    for (int j = 0; j < na; ++j) {
+      const int2 bwin = tb[w][j];
+      V win[WMAX];
+#pragma unroll
+      for (int jj = 0; jj < WMAX; ++jj) {
+        const int bin = bwin.x - 1 + jj;
+        win[jj] = ld_or_zero<V>(yang + (ptrdiff_t)bin * g.Hy,
+                                hv && jj < bwin.y && (unsigned)bin < (unsigned)g.PX);
+      }
+#pragma unroll
+      for (int v = 0; v < NV; ++v) {
+        const float4 e = tw[w][j][v];
+        // offsets outside [0, OMAX] cannot occur (see BlockWindow) and would
+        // match no case
+        apply_window<0, OMAX>(acc[v], e, win, __float_as_int(e.w) - bwin.x);
+      }
+      yang += yrow_stride;
+    }
+    __syncwarp();
+  }
+
+  if (hv) {
+#pragma unroll
+    for (int v = 0; v < NV; ++v) {
+      const int xi = xi0 + v % BX;
+      const int yi = yi0 + v / BX;
+      if (xi < g.SX && yi < g.SY) {
+        V* px = reinterpret_cast<V*>(x + ((size_t)yi * g.SX + xi) * g.Hx + h);
+        store_out(px, acc[v], g.accumulate);
       }
     }
   }
@@ -195,7 +323,7 @@ __global__ void __launch_bounds__(32 * BP2_WARPS)
       const int h = h0 + i;
       if (h < g.H) {
         float* px = x + ((size_t)h * g.SY + yi) * g.SX + xi;
-        *px += acc[i];
+        store_out(px, acc[i], g.accumulate);
       }
     }
   }
@@ -205,10 +333,33 @@ inline unsigned ceil_div(long long a, long long b) { return (unsigned)((a + b - 
 
 }  // namespace
 
+template <int BX, int BY>
+cudaError_t launch_bp_z0_block(const float* y, float* x, const float* angles, const Geom& g,
+                               cudaStream_t stream) {
+  const int nbx = (g.SX + BX - 1) / BX;
+  const int nby = (g.SY + BY - 1) / BY;
+  const long long nblocks = (long long)nbx * nby;
+  dim3 block(32, BPB_WARPS);
+  dim3 grid(ceil_div(g.H, 128), ceil_div(nblocks, BPB_WARPS));
+  bp_z0_block_kernel<BX, BY><<<grid, block, 0, stream>>>(y, x, angles, g, nbx, (int)nblocks);
+  return cudaGetLastError();
+}
+
+// Variants: 1 = one voxel run per warp (bp_z0_kernel); 2 = 4x4 register
+// block (default when heights come in float4); 3 = 4x2; 4 = 2x2; 5 = 8x2.
 cudaError_t launch_backward_z0(const float* y, float* x, const float* angles, const Geom& g,
                                cudaStream_t stream) {
   const bool vec4 = (g.Hx % 4 == 0) && (g.Hy % 4 == 0) &&
                     ((reinterpret_cast<uintptr_t>(x) | reinterpret_cast<uintptr_t>(y)) & 15) == 0;
+  const int variant = kernel_variant(OP_BACKWARD_Z0);
+  if (vec4 && variant != 1) {
+    switch (variant) {
+      case 3: return launch_bp_z0_block<4, 2>(y, x, angles, g, stream);
+      case 4: return launch_bp_z0_block<2, 2>(y, x, angles, g, stream);
+      case 5: return launch_bp_z0_block<8, 2>(y, x, angles, g, stream);
+      default: return launch_bp_z0_block<4, 4>(y, x, angles, g, stream);
+    }
+  }
   const int R = vec4 ? 4 : 1;
   dim3 block(32, BP0_WARPS);
   dim3 grid(ceil_div(g.H, 32 * R), ceil_div(g.SX, BP0_RUN), ceil_div(g.SY, BP0_WARPS));

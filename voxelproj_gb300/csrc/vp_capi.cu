@@ -6,6 +6,7 @@
 
 #include <atomic>
 #include <cstdint>
+#include <mutex>
 
 #include "../../include/voxelproj_gb300.h"
 #include "vp_common.cuh"
@@ -15,6 +16,7 @@ namespace {
 
 thread_local int g_last_cuda_error = 0;
 std::atomic<uint64_t> g_launches{0};
+std::atomic<int> g_variant[vp::OP_COUNT] = {};
 
 constexpr int64_t kMaxDim = (int64_t)1 << 30;
 // fp_z0 packs the voxel index (yi*SX + xi) with 3 tag bits into an int.
@@ -52,7 +54,37 @@ int make_geom(const void* xp, int64_t SY, int64_t SX, int64_t Hx, const void* yp
   g->ycent = 0.5f * (float)(SY - 1);
   g->pcent = 0.5f * (float)(PX - 1);
   g->trig = (flags & VP_FLAG_TRIG_PRECISE) ? vp::TRIG_PRECISE : vp::TRIG_REF;
+  g->accumulate = 1;
   return VP_OK;
+}
+
+// Library-private stream-ordered pool for z_order 2 scratch when the caller
+// supplies none; it keeps freed memory (release threshold = max) so repeated
+// calls do not go back to the driver.
+constexpr int kMaxDevices = 64;
+std::mutex g_pool_mutex;
+cudaMemPool_t g_pools[kMaxDevices] = {};
+
+cudaError_t private_pool(cudaMemPool_t* out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> lock(g_pool_mutex);
+  if (g_pools[dev] == nullptr) {
+    cudaMemPoolProps props = {};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = dev;
+    cudaMemPool_t pool;
+    e = cudaMemPoolCreate(&pool, &props);
+    if (e != cudaSuccess) return e;
+    uint64_t keep = UINT64_MAX;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    g_pools[dev] = pool;
+  }
+  *out = g_pools[dev];
+  return cudaSuccess;
 }
 
 int finish(cudaError_t e, int launches) {
@@ -66,7 +98,22 @@ int finish(cudaError_t e, int launches) {
 
 }  // namespace
 
+namespace vp {
+int kernel_variant(int op) {
+  return (op >= 0 && op < OP_COUNT) ? g_variant[op].load(std::memory_order_relaxed) : 0;
+}
+}  // namespace vp
+
 extern "C" {
+
+int vp_set_kernel_variant(int op, int variant) {
+  if (op < 0 || op >= vp::OP_COUNT || variant < 0 || variant > 64) return VP_ERR_BAD_FLAGS;
+  g_variant[op].store(variant, std::memory_order_relaxed);
+  return VP_OK;
+}
+
+int vp_get_kernel_variant(int op) { return vp::kernel_variant(op); }
+
 
 int vp_version(void) { return 100; }
 
@@ -79,6 +126,7 @@ const char* vp_error_string(int status) {
     case VP_ERR_CUDA: return "CUDA runtime error";
     case VP_ERR_BAD_FLAGS: return "unknown flag bits";
     case VP_ERR_BAD_Z_ORDER: return "z_order must be 0 or 2";
+    case VP_ERR_WORKSPACE: return "workspace smaller than vp_z2_workspace_bytes()";
     default: return "unknown status";
   }
 }
@@ -110,28 +158,89 @@ int vp_backward_z0(const float* y, int64_t y0, int64_t y1, int64_t y2, float* x,
   return finish(vp::launch_backward_z0(y, x, angles, g, (cudaStream_t)stream), 1);
 }
 
-int vp_forward_z2(const float* x, int64_t x0, int64_t x1, int64_t x2, float* y, int64_t y0,
-                  int64_t y1, int64_t y2, const float* angles, int64_t n_angles, int flags,
-                  void* stream) {
+size_t vp_z2_workspace_bytes(int64_t x0, int64_t x1, int64_t x2, int64_t y0, int64_t y1,
+                             int64_t y2) {
+  vp::Geom g;
+  bool empty = false;
+  const float one = 0.f;
+  // shapes only: dummy non-null pointers, all angles assumed present
+  if (make_geom(&one, x1, x2, x0, &one, y1, y2, y0, &one, y1, 0, &g, &empty) != VP_OK || empty)
+    return 0;
+  return vp::z2_workspace_bytes(g);
+}
+
+}  // extern "C"
+
+namespace {
+
+// z_order 2 dispatch shared by the entry points with and without workspace.
+int run_z2(bool forward, const float* in, float* out, const float* angles, const vp::Geom& g,
+           void* ws, size_t ws_bytes, cudaStream_t stream) {
+  if (!vp::z2_uses_transpose(g)) {
+    cudaError_t e = forward ? vp::launch_forward_z2(in, out, angles, g, stream)
+                            : vp::launch_backward_z2(in, out, angles, g, stream);
+    return finish(e, vp::launches_z2(g, forward));
+  }
+  const size_t need = vp::z2_workspace_bytes(g);
+  bool owned = false;
+  if (ws == nullptr) {
+    cudaMemPool_t pool;
+    cudaError_t e = private_pool(&pool);
+    if (e == cudaSuccess) e = cudaMallocFromPoolAsync(&ws, need, pool, stream);
+    if (e != cudaSuccess) return finish(e, 0);
+    owned = true;
+  } else if (ws_bytes < need) {
+    return VP_ERR_WORKSPACE;
+  }
+  cudaError_t e = forward
+      ? vp::forward_z2_transposed(in, out, angles, g, static_cast<float*>(ws), stream)
+      : vp::backward_z2_transposed(in, out, angles, g, static_cast<float*>(ws), stream);
+  if (owned) {
+    const cudaError_t f = cudaFreeAsync(ws, stream);
+    if (e == cudaSuccess) e = f;
+  }
+  return finish(e, vp::launches_z2(g, forward));
+}
+
+}  // namespace
+
+extern "C" {
+
+int vp_forward_z2_ws(const float* x, int64_t x0, int64_t x1, int64_t x2, float* y, int64_t y0,
+                     int64_t y1, int64_t y2, const float* angles, int64_t n_angles, int flags,
+                     void* workspace, size_t workspace_bytes, void* stream) {
   vp::Geom g;
   bool empty = false;
   // z_order 2: x (Hx, SY, SX), y (Hy, n_ang, PX)
   if (int s = make_geom(x, x1, x2, x0, y, y1, y2, y0, angles, n_angles, flags, &g, &empty))
     return s;
   if (empty) return VP_OK;
-  return finish(vp::launch_forward_z2(x, y, angles, g, (cudaStream_t)stream),
-                vp::launches_forward_z2(g));
+  return run_z2(true, x, y, angles, g, workspace, workspace_bytes, (cudaStream_t)stream);
 }
 
-int vp_backward_z2(const float* y, int64_t y0, int64_t y1, int64_t y2, float* x, int64_t x0,
-                   int64_t x1, int64_t x2, const float* angles, int64_t n_angles, int flags,
-                   void* stream) {
+int vp_backward_z2_ws(const float* y, int64_t y0, int64_t y1, int64_t y2, float* x, int64_t x0,
+                      int64_t x1, int64_t x2, const float* angles, int64_t n_angles, int flags,
+                      void* workspace, size_t workspace_bytes, void* stream) {
   vp::Geom g;
   bool empty = false;
   if (int s = make_geom(x, x1, x2, x0, y, y1, y2, y0, angles, n_angles, flags, &g, &empty))
     return s;
   if (empty) return VP_OK;
-  return finish(vp::launch_backward_z2(y, x, angles, g, (cudaStream_t)stream), 1);
+  return run_z2(false, y, x, angles, g, workspace, workspace_bytes, (cudaStream_t)stream);
+}
+
+int vp_forward_z2(const float* x, int64_t x0, int64_t x1, int64_t x2, float* y, int64_t y0,
+                  int64_t y1, int64_t y2, const float* angles, int64_t n_angles, int flags,
+                  void* stream) {
+  return vp_forward_z2_ws(x, x0, x1, x2, y, y0, y1, y2, angles, n_angles, flags, nullptr, 0,
+                          stream);
+}
+
+int vp_backward_z2(const float* y, int64_t y0, int64_t y1, int64_t y2, float* x, int64_t x0,
+                   int64_t x1, int64_t x2, const float* angles, int64_t n_angles, int flags,
+                   void* stream) {
+  return vp_backward_z2_ws(y, y0, y1, y2, x, x0, x1, x2, angles, n_angles, flags, nullptr, 0,
+                           stream);
 }
 
 int vp_forward(const float* x, const int64_t x_dims[3], float* y, const int64_t y_dims[3],

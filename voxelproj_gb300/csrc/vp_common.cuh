@@ -87,9 +87,20 @@ __device__ __forceinline__ float trap_cdf(float x, float a, float b, float coeff
   return r;
 }
 
-// Detector coordinate of a voxel with centred coordinates (relx, rely).
+// Detector coordinate of a voxel with centred coordinates (relx, rely), in
+// one fixed rounding order so every kernel (and both directions) computes
+// bit-identical weights.  VP_XP_FORM selects which product is fused.
+#ifndef VP_XP_FORM
+#define VP_XP_FORM 0
+#endif
 __device__ __forceinline__ float det_coord(float relx, float rely, float c, float s, float pcent) {
+#if VP_XP_FORM == 1
+  return __fadd_rn(__fmaf_rn(relx, c, __fmul_rn(rely, s)), pcent);
+#elif VP_XP_FORM == 2
+  return __fadd_rn(__fmaf_rn(rely, s, __fmul_rn(relx, c)), pcent);
+#else
   return relx * c + rely * s + pcent;
+#endif
 }
 
 // Weights of bins r-1, r, r+1 for a voxel projecting to xp
@@ -185,6 +196,15 @@ struct Geom {
   int Hx, Hy;       // height extent of x and of y (z_order 0 row strides)
   float xcent, ycent, pcent;
   int trig;
+  int accumulate;   // 1: out += result (the reference's semantics); 0: out = result
 };
+
+// Epilogue: out (+)= acc.
+__device__ __forceinline__ void store_out(float4* p, float4 v, int accumulate) {
+  *p = accumulate ? f4_add(*p, v) : v;
+}
+__device__ __forceinline__ void store_out(float* p, float v, int accumulate) {
+  *p = accumulate ? *p + v : v;
+}
 
 }  // namespace vp

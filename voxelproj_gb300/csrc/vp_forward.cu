@@ -175,7 +175,7 @@ __global__ void __launch_bounds__(32 * FP0_WARPS)
       const int p = p0 + b;
       if (p < g.PX) {
         V* py = reinterpret_cast<V*>(y + ((size_t)a * g.PX + p) * g.Hy + h);
-        *py = f4_add(*py, acc[b]);
+        store_out(py, acc[b], g.accumulate);
       }
     }
   }
@@ -242,7 +242,7 @@ __global__ void __launch_bounds__(32 * FP2_WARPS)
 #pragma unroll
     for (int r = 0; r < FP2_RH; ++r) {
       const int h = h0 + r;
-      if (h < g.H) y[(size_t)h * yh_stride + (size_t)a * g.PX + p] += acc[r];
+      if (h < g.H) store_out(y + (size_t)h * yh_stride + (size_t)a * g.PX + p, acc[r], g.accumulate);
     }
   }
 }

@@ -20,6 +20,20 @@ cudaError_t launch_backward_z0(const float* y, float* x, const float* angles, co
 cudaError_t launch_backward_z2(const float* y, float* x, const float* angles, const Geom& g,
                                cudaStream_t stream);
 
+// Kernel variant selection (0 = automatic), set through vp_set_kernel_variant.
+enum Op : int { OP_FORWARD_Z0 = 0, OP_BACKWARD_Z0 = 1, OP_FORWARD_Z2 = 2, OP_BACKWARD_Z2 = 3,
+                OP_COUNT = 4 };
+int kernel_variant(int op);
+
+// z_order 2 through the z_order 0 kernels (vp_z2.cu).
+bool z2_uses_transpose(const Geom& g);
+size_t z2_workspace_bytes(const Geom& g);
+int launches_z2(const Geom& g, bool forward);
+cudaError_t forward_z2_transposed(const float* x, float* y, const float* angles, const Geom& g,
+                                  float* ws, cudaStream_t stream);
+cudaError_t backward_z2_transposed(const float* y, float* x, const float* angles, const Geom& g,
+                                   float* ws, cudaStream_t stream);
+
 // Kernel launches the forward launchers issue for a geometry (grids are
 // split past 65535 angle blocks).
 int launches_forward_z0(const Geom& g);

@@ -1,0 +1,131 @@
+// z_order 2 through the z_order 0 kernels.
+//
+// In z_order 2 the height axis is the slowest one: x (H, SY, SX) and
+// y (H, n_ang, PX).  The projector's weights do not depend on the height,
+// so the fast kernels put heights across the lanes of a warp; that needs
+// heights contiguous.  For H >= 32 the z_order 2 operators therefore run as
+//     transpose the input to height-fastest order  (HBM-bound tiled transpose)
+//     z_order 0 kernel, storing (not accumulating) into scratch
+//     transpose the result back, adding it to the caller's output
+// which costs about 2 * (|x| + |y|) of extra HBM traffic, a fraction of a
+// millisecond at 512^3 against several milliseconds of projector work, and
+// keeps the reference's accumulate semantics.  Small H keeps the native
+// z_order 2 kernels (lanes across x / PX).
+//
+// Scratch: SY*SX*Hp + n_ang*PX*Hp floats (Hp = H rounded up to 4), supplied by
+// the caller (vp_*_z2_ws) or taken from a library-private stream-ordered pool.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "vp_common.cuh"
+#include "vp_launch.h"
+
+namespace vp {
+
+namespace {
+
+constexpr int TT = 32;         // tile edge
+constexpr int TROWS = 8;       // thread rows per tile (each thread moves TT/TROWS elements)
+
+// dst[c * dst_ld + r] (+)= src[r * src_ld + c] for r < rows, c < cols.
+// Tiles are visited with a grid-stride loop so any matrix fits one launch.
+__global__ void __launch_bounds__(TT * TROWS)
+    transpose_kernel(const float* __restrict__ src, float* __restrict__ dst, long long rows,
+                     long long cols, long long src_ld, long long dst_ld, int accumulate) {
+  __shared__ float tile[TT][TT + 1];
+  const long long tiles_c = (cols + TT - 1) / TT;
+  const long long tiles_r = (rows + TT - 1) / TT;
+  const long long ntiles = tiles_c * tiles_r;
+  for (long long t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const long long r0 = (t / tiles_c) * TT;
+    const long long c0 = (t % tiles_c) * TT;
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < TT; i += TROWS) {
+      const long long r = r0 + threadIdx.y + i;
+      const long long c = c0 + threadIdx.x;
+      if (r < rows && c < cols) tile[threadIdx.y + i][threadIdx.x] = __ldg(src + r * src_ld + c);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < TT; i += TROWS) {
+      const long long c = c0 + threadIdx.y + i;
+      const long long r = r0 + threadIdx.x;
+      if (r < rows && c < cols) {
+        float* p = dst + c * dst_ld + r;
+        const float v = tile[threadIdx.x][threadIdx.y + i];
+        *p = accumulate ? *p + v : v;
+      }
+    }
+  }
+}
+
+cudaError_t transpose(const float* src, float* dst, long long rows, long long cols,
+                      long long src_ld, long long dst_ld, int accumulate, cudaStream_t stream) {
+  if (rows <= 0 || cols <= 0) return cudaSuccess;
+  const long long ntiles = ((rows + TT - 1) / TT) * ((cols + TT - 1) / TT);
+  int dev = 0, sms = 152;
+  if (cudaGetDevice(&dev) == cudaSuccess)
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const long long cap = (long long)sms * 8;
+  const unsigned grid = (unsigned)(ntiles < cap ? ntiles : cap);
+  transpose_kernel<<<grid, dim3(TT, TROWS), 0, stream>>>(src, dst, rows, cols, src_ld, dst_ld,
+                                                        accumulate);
+  return cudaGetLastError();
+}
+
+inline long long round4(long long v) { return (v + 3) / 4 * 4; }
+
+}  // namespace
+
+bool z2_uses_transpose(const Geom& g) { return g.H >= 32; }
+
+size_t z2_workspace_bytes(const Geom& g) {
+  if (!z2_uses_transpose(g)) return 0;
+  const long long Hp = round4(g.H);
+  return (size_t)(((long long)g.SY * g.SX + (long long)g.n_ang * g.PX) * Hp) * sizeof(float);
+}
+
+int launches_z2(const Geom& g, bool forward) {
+  if (!z2_uses_transpose(g)) return forward ? launches_forward_z2(g) : 1;
+  return 2 + (forward ? launches_forward_z0(g) : 1);
+}
+
+// x (Hx, SY, SX) -> xt (SY, SX, Hp); yt = A xt; y (Hy, n, PX) += yt^T.
+cudaError_t forward_z2_transposed(const float* x, float* y, const float* angles, const Geom& g,
+                                  float* ws, cudaStream_t stream) {
+  const long long Hp = round4(g.H);
+  const long long nvox = (long long)g.SY * g.SX;
+  const long long nbin = (long long)g.n_ang * g.PX;
+  float* xt = ws;
+  float* yt = ws + nvox * Hp;
+  cudaError_t e = transpose(x, xt, g.H, nvox, nvox, Hp, 0, stream);
+  if (e != cudaSuccess) return e;
+  Geom g0 = g;
+  g0.H = g0.Hx = g0.Hy = (int)Hp;
+  g0.accumulate = 0;
+  e = launch_forward_z0(xt, yt, angles, g0, stream);
+  if (e != cudaSuccess) return e;
+  return transpose(yt, y, nbin, g.H, Hp, nbin, 1, stream);
+}
+
+// y (Hy, n, PX) -> yt (n, PX, Hp); xt = A^T yt; x (Hx, SY, SX) += xt^T.
+cudaError_t backward_z2_transposed(const float* y, float* x, const float* angles, const Geom& g,
+                                   float* ws, cudaStream_t stream) {
+  const long long Hp = round4(g.H);
+  const long long nvox = (long long)g.SY * g.SX;
+  const long long nbin = (long long)g.n_ang * g.PX;
+  float* xt = ws;
+  float* yt = ws + nvox * Hp;
+  cudaError_t e = transpose(y, yt, g.H, nbin, nbin, Hp, 0, stream);
+  if (e != cudaSuccess) return e;
+  Geom g0 = g;
+  g0.H = g0.Hx = g0.Hy = (int)Hp;
+  g0.accumulate = 0;
+  e = launch_backward_z0(yt, xt, angles, g0, stream);
+  if (e != cudaSuccess) return e;
+  return transpose(xt, x, nvox, g.H, Hp, nvox, 1, stream);
+}
+
+}  // namespace vp

@@ -56,6 +56,10 @@ def parse_args():
     ap.add_argument("--angles", type=int, default=192)
     ap.add_argument("--z-order", type=int, default=0, choices=[0, 2])
     ap.add_argument("--trig", choices=["reference", "precise"], default="reference")
+    ap.add_argument("--variant-fwd", type=int, default=0,
+                    help="kernel variant for A (0 = library default)")
+    ap.add_argument("--variant-bwd", type=int, default=0,
+                    help="kernel variant for A^T (0 = library default)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=10.0,
@@ -260,6 +264,7 @@ def workload_config(args):
         "l2": "inputs larger than L2 (x %d MB, y %d MB > 129 MB L2)"
               % (S**3 * 4 // 2**20, n * S * S * 4 // 2**20),
         "parallelism": "replicas (one independent problem per GPU)",
+        "kernel_variants": {"A": args.variant_fwd or "default", "AT": args.variant_bwd or "default"},
     }
 
 
@@ -274,6 +279,9 @@ def run_ours(args, world, rank, local):
     if world > 1:
         torch.distributed.init_process_group("nccl", device_id=dev)
     vp.set_trig_mode(args.trig)
+    op_f, op_b = (0, 1) if args.z_order == 0 else (2, 3)
+    _lib.LIB.vp_set_kernel_variant(op_f, args.variant_fwd)
+    _lib.LIB.vp_set_kernel_variant(op_b, args.variant_bwd)
     S, n, z = args.size, args.angles, args.z_order
     PX = S
     xs, ys = shapes(S, n, z)

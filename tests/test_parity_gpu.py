@@ -132,3 +132,54 @@ def test_weight_sum_single_voxel():
         y = vp.forward(torch.tensor(x, device="cuda"), ang, (n, 16, H))
         sums = y.sum(dim=(1, 2)).cpu().numpy() / H
         assert np.abs(sums - 1).max() < 2e-6
+
+
+# Every kernel variant of the z_order 0 adjoint against the oracle (the
+# autotuner may pick any of them): sizes that are not multiples of the block
+# or run shape, degenerate angles, both signs of each step, several height
+# chunks.
+@pytest.mark.parametrize("variant", [1, 2, 3, 4, 5, 6])
+@pytest.mark.parametrize("geom", [(23, 37, 132, 61, 50, "wide"), (9, 6, 8, 40, 11, "axes"),
+                                  (64, 64, 256, 96, 64, "rand")],
+                         ids=lambda g: "x".join(map(str, g[:5])) + g[5])
+def test_backward_variants(variant, geom):
+    from voxelproj_gb300 import _lib
+
+    SY, SX, H, n, PX, kind = geom
+    ang = angle_set(kind, n, 99)
+    y = seeded((n, PX, H), 31)
+    x0 = seeded((SY, SX, H), 32)
+    _lib.LIB.vp_set_kernel_variant(1, variant)
+    try:
+        xo = torch.tensor(x0, device="cuda")
+        vp._CU.backward_z0(torch.tensor(y, device="cuda"), xo, torch.tensor(ang, device="cuda"))
+        torch.cuda.synchronize()
+    finally:
+        _lib.LIB.vp_set_kernel_variant(1, 0)
+    err = rel_err(xo.cpu().numpy() - x0, oracle.backward(y, ang, SY, SX, 0))
+    print(f"\n[variant {variant}] {geom}: A^T {err:.3e}")
+    assert err <= tol.ref_vs_fp64(max(SY, SX, PX))
+
+
+@pytest.mark.parametrize("variant", [1, 4, 6])
+def test_backward_variants_store_mode_via_z2(variant):
+    """z_order 2 with H >= 32 runs the z_order 0 kernel in store mode into
+    scratch; the result must not depend on the scratch's prior content."""
+    from voxelproj_gb300 import _lib
+
+    SY, SX, H, n, PX = 20, 26, 36, 30, 34
+    ang = lin(n)
+    y = seeded((H, n, PX), 41)
+    x0 = seeded((H, SY, SX), 42)
+    _lib.LIB.vp_set_kernel_variant(1, variant)
+    try:
+        outs = []
+        for _ in range(2):
+            xo = torch.tensor(x0, device="cuda")
+            vp._CU.backward_z2(torch.tensor(y, device="cuda"), xo, torch.tensor(ang, device="cuda"))
+            torch.cuda.synchronize()
+            outs.append(xo.cpu().numpy())
+    finally:
+        _lib.LIB.vp_set_kernel_variant(1, 0)
+    np.testing.assert_array_equal(outs[0], outs[1])
+    assert rel_err(outs[0] - x0, oracle.backward(y, ang, SY, SX, 2)) <= tol.ref_vs_fp64(PX)

@@ -58,9 +58,9 @@ __global__ void __launch_bounds__(32 * BP0_WARPS)
 
   const int lane = threadIdx.x;
   const int w = threadIdx.y;
-  const int h = (blockIdx.x * 32 + lane) * R;
-  const int xi0 = blockIdx.y * BP0_RUN;
-  const int yi = blockIdx.z * BP0_WARPS + w;
+  const int xi0 = blockIdx.x * BP0_RUN;
+  const int yi = blockIdx.y * BP0_WARPS + w;
+  const int h = (blockIdx.z * 32 + lane) * R;
   if (yi >= g.SY) return;  // warp-uniform; the table is per warp
   const bool hv = h < g.H;
 
@@ -176,8 +176,8 @@ __global__ void __launch_bounds__(32 * BPB_WARPS)
 
   const int lane = threadIdx.x;
   const int w = threadIdx.y;
-  const int h = (blockIdx.x * 32 + lane) * 4;
-  const int bidx = blockIdx.y * BPB_WARPS + w;
+  const int bidx = blockIdx.x * BPB_WARPS + w;
+  const int h = (blockIdx.y * 32 + lane) * 4;
   if (bidx >= nblocks) return;  // warp-uniform; tables are per warp
   const int xi0 = (bidx % nbx) * BX;
   const int yi0 = (bidx / nbx) * BY;
@@ -238,6 +238,187 @@ __global__ void __launch_bounds__(32 * BPB_WARPS)
       if (xi < g.SX && yi < g.SY) {
         V* px = reinterpret_cast<V*>(x + ((size_t)yi * g.SX + xi) * g.Hx + h);
         store_out(px, acc[v], g.accumulate);
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// z_order 0, run kernel.  Angles split in two classes: in class X (|c| <=
+// |s|) one step along x moves xp by |c| <= sqrt(1/2), in class Y (|c| > |s|)
+// one step along y moves it by |s| < sqrt(1/2).  One launch per class; in
+// each, a warp owns RUN = 4 voxels along that axis and 128 heights (lane <->
+// 4 heights) and visits only the angles of its class.
+//
+// Along the run xp advances by less than one bin per voxel, so round(xp)
+// advances by 0 or 1 per voxel (mirrored when the step is negative: the
+// window is then read in decreasing bin order and w0/w2 swap places).  The
+// run's bins form a window of W = 3 + (number of advances) <= 6 bins that is
+// loaded once, and the pattern of advances (3 bits) selects one of 8
+// straight-line code paths with static register indices: one warp-uniform
+// branch per run and angle.  Float noise can break monotonicity when xp sits
+// on a half-integer and the step is tiny; such (run, angle) pairs take a
+// generic path with three loads per voxel.
+//
+// Angles of a class are compacted per chunk (ballot + prefix count).  Table
+// per (run, angle): 12 weights in window order, the 4 bins r, and
+// (base bin, direction, pattern).  The second launch adds into x; a warp that
+// saw no angle of its class leaves x untouched (in store mode the first launch
+// always writes).
+// ---------------------------------------------------------------------------
+constexpr int RUN = 4;
+constexpr int BPR_WARPS = 4;
+constexpr int BPR_CHUNK = 32;
+constexpr int BPR_GENERIC = 8;  // pattern value of the generic path
+
+struct RunEntry {
+  float4 w[3];  // weights of voxels 0..3, 3 each, in window order
+  int4 r;       // bin round(xp) of each voxel
+  int4 meta;    // base bin of the window, direction (+1/-1), pattern, angle index
+};
+
+template <int PAT>
+__device__ __forceinline__ void run_apply(float4 (&acc)[RUN], const float4 (&wv)[3],
+                                          const float4 (&win)[6]) {
+  constexpr int o1 = (PAT & 1);
+  constexpr int o2 = o1 + ((PAT >> 1) & 1);
+  constexpr int o3 = o2 + ((PAT >> 2) & 1);
+  const float ws[12] = {wv[0].x, wv[0].y, wv[0].z, wv[0].w, wv[1].x, wv[1].y,
+                        wv[1].z, wv[1].w, wv[2].x, wv[2].y, wv[2].z, wv[2].w};
+  constexpr int off[RUN] = {0, o1, o2, o3};
+#pragma unroll
+  for (int m = 0; m < RUN; ++m) {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) acc[m] = f4_fma(ws[3 * m + k], win[off[m] + k], acc[m]);
+  }
+}
+
+template <int PASS>
+__global__ void __launch_bounds__(32 * BPR_WARPS)
+    bp_z0_runs_kernel(const float* __restrict__ y, float* __restrict__ x,
+                      const float* __restrict__ angles, Geom g, int nrun_major, int nruns,
+                      int accumulate) {
+  __shared__ RunEntry tab[BPR_WARPS][BPR_CHUNK];
+
+  const int lane = threadIdx.x;
+  const int w = threadIdx.y;
+  const int run = blockIdx.x * BPR_WARPS + w;
+  if (run >= nruns) return;  // warp-uniform; tables are per warp
+  const int h = (blockIdx.y * 32 + lane) * 4;
+  const bool hv = h < g.H;
+  // PASS 0: run along x starting at (xi0, yi0); PASS 1: along y.
+  const int xi0 = PASS == 0 ? (run % nrun_major) * RUN : run % nrun_major;
+  const int yi0 = PASS == 0 ? run / nrun_major : (run / nrun_major) * RUN;
+  const int dx = PASS == 0 ? 1 : 0;
+  const int dy = PASS == 0 ? 0 : 1;
+
+  float4 acc[RUN];
+#pragma unroll
+  for (int m = 0; m < RUN; ++m) acc[m] = vzero<float4>();
+
+  const size_t yrow_stride = (size_t)g.PX * g.Hy;
+  int seen = 0;
+
+  for (int a0 = 0; a0 < g.n_ang; a0 += BPR_CHUNK) {
+    const int a = a0 + lane;
+    bool mine = false;
+    AngleConst k;
+    if (a < g.n_ang) {
+      k = angle_const(angles[a], g.trig);
+      const bool class_x = fabsf(k.c) <= fabsf(k.s);
+      mine = (PASS == 0) == class_x;
+    }
+    const unsigned mask = __ballot_sync(0xffffffffu, mine);
+    const int count = __popc(mask);
+    if (mine) {
+      const int slot = __popc(mask & ((1u << lane) - 1u));
+      BinWeights bw[RUN];
+#pragma unroll
+      for (int m = 0; m < RUN; ++m) {
+        const float relx = (float)(xi0 + m * dx) - g.xcent;
+        const float rely = (float)(yi0 + m * dy) - g.ycent;
+        bw[m] = voxel_weights(relx, rely, k, g.pcent, g.trig);
+      }
+      const float step = PASS == 0 ? k.c : k.s;
+      const int dir = step >= 0.0f ? 1 : -1;
+      int pattern = 0;
+      bool ok = true;
+#pragma unroll
+      for (int m = 0; m + 1 < RUN; ++m) {
+        const int d = dir * (bw[m + 1].r - bw[m].r);
+        ok = ok && (d == 0 || d == 1);
+        pattern |= (d == 1 ? 1 : 0) << m;
+      }
+      RunEntry e;
+      float ws[12];
+#pragma unroll
+      for (int m = 0; m < RUN; ++m) {
+        // window order: increasing u, bin = base + dir * u
+        ws[3 * m + 0] = dir > 0 ? bw[m].w0 : bw[m].w2;
+        ws[3 * m + 1] = bw[m].w1;
+        ws[3 * m + 2] = dir > 0 ? bw[m].w2 : bw[m].w0;
+      }
+      e.w[0] = make_float4(ws[0], ws[1], ws[2], ws[3]);
+      e.w[1] = make_float4(ws[4], ws[5], ws[6], ws[7]);
+      e.w[2] = make_float4(ws[8], ws[9], ws[10], ws[11]);
+      e.r = make_int4(bw[0].r, bw[1].r, bw[2].r, bw[3].r);
+      e.meta = make_int4(bw[0].r - dir, dir, ok ? pattern : BPR_GENERIC, a);
+      tab[w][slot] = e;
+    }
+    __syncwarp();
+    const float* yang_base = y + h;
+    for (int j = 0; j < count; ++j) {
+      const RunEntry& e = tab[w][j];
+      const int4 meta = e.meta;
+      const float4 wv[3] = {e.w[0], e.w[1], e.w[2]};
+      const float* yang = yang_base + (size_t)meta.w * yrow_stride;
+      if (meta.z != BPR_GENERIC) {
+        const int W = 3 + __popc(meta.z);
+        float4 win[6];
+#pragma unroll
+        for (int u = 0; u < 6; ++u) {
+          const int bin = meta.x + meta.y * u;
+          win[u] = ld_or_zero<float4>(yang + (ptrdiff_t)bin * g.Hy,
+                                      hv && u < W && (unsigned)bin < (unsigned)g.PX);
+        }
+        switch (meta.z) {
+          case 0: run_apply<0>(acc, wv, win); break;
+          case 1: run_apply<1>(acc, wv, win); break;
+          case 2: run_apply<2>(acc, wv, win); break;
+          case 3: run_apply<3>(acc, wv, win); break;
+          case 4: run_apply<4>(acc, wv, win); break;
+          case 5: run_apply<5>(acc, wv, win); break;
+          case 6: run_apply<6>(acc, wv, win); break;
+          default: run_apply<7>(acc, wv, win); break;
+        }
+      } else {
+        const int rr[RUN] = {e.r.x, e.r.y, e.r.z, e.r.w};
+        const float ws[12] = {wv[0].x, wv[0].y, wv[0].z, wv[0].w, wv[1].x, wv[1].y,
+                              wv[1].z, wv[1].w, wv[2].x, wv[2].y, wv[2].z, wv[2].w};
+#pragma unroll
+        for (int m = 0; m < RUN; ++m) {
+#pragma unroll
+          for (int kk = 0; kk < 3; ++kk) {
+            const int bin = rr[m] + meta.y * (kk - 1);
+            const float4 v = ld_or_zero<float4>(yang + (ptrdiff_t)bin * g.Hy,
+                                                hv && (unsigned)bin < (unsigned)g.PX);
+            acc[m] = f4_fma(ws[3 * m + kk], v, acc[m]);
+          }
+        }
+      }
+    }
+    seen += count;
+    __syncwarp();
+  }
+
+  if (hv && (seen > 0 || !accumulate)) {
+#pragma unroll
+    for (int m = 0; m < RUN; ++m) {
+      const int xi = xi0 + m * dx;
+      const int yi = yi0 + m * dy;
+      if (xi < g.SX && yi < g.SY) {
+        float4* px = reinterpret_cast<float4*>(x + ((size_t)yi * g.SX + xi) * g.Hx + h);
+        store_out(px, acc[m], accumulate);
       }
     }
   }
@@ -340,29 +521,56 @@ cudaError_t launch_bp_z0_block(const float* y, float* x, const float* angles, co
   const int nby = (g.SY + BY - 1) / BY;
   const long long nblocks = (long long)nbx * nby;
   dim3 block(32, BPB_WARPS);
-  dim3 grid(ceil_div(g.H, 128), ceil_div(nblocks, BPB_WARPS));
+  // heights slowest, so blocks running together share one 128-height chunk
+  dim3 grid(ceil_div(nblocks, BPB_WARPS), ceil_div(g.H, 128));
   bp_z0_block_kernel<BX, BY><<<grid, block, 0, stream>>>(y, x, angles, g, nbx, (int)nblocks);
   return cudaGetLastError();
 }
 
+cudaError_t launch_bp_z0_runs(const float* y, float* x, const float* angles, const Geom& g,
+                              cudaStream_t stream) {
+  dim3 block(32, BPR_WARPS);
+  const unsigned hchunks = ceil_div(g.H, 128);
+  const int nmaj0 = (int)ceil_div(g.SX, RUN);
+  const long long nruns0 = (long long)nmaj0 * g.SY;
+  bp_z0_runs_kernel<0><<<dim3(ceil_div(nruns0, BPR_WARPS), hchunks), block, 0, stream>>>(
+      y, x, angles, g, nmaj0, (int)nruns0, g.accumulate);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  const long long nruns1 = (long long)g.SX * ceil_div(g.SY, RUN);
+  bp_z0_runs_kernel<1><<<dim3(ceil_div(nruns1, BPR_WARPS), hchunks), block, 0, stream>>>(
+      y, x, angles, g, g.SX, (int)nruns1, 1);
+  return cudaGetLastError();
+}
+
+bool bp0_vec4(const float* y, const float* x, const Geom& g) {
+  return (g.Hx % 4 == 0) && (g.Hy % 4 == 0) &&
+         ((reinterpret_cast<uintptr_t>(x) | reinterpret_cast<uintptr_t>(y)) & 15) == 0;
+}
+
+int launches_backward_z0(const float* y, const float* x, const Geom& g) {
+  return (bp0_vec4(y, x, g) && kernel_variant(OP_BACKWARD_Z0) == 6) ? 2 : 1;
+}
+
 // Variants: 1 = one voxel run per warp (bp_z0_kernel); 2 = 4x4 register
-// block (default when heights come in float4); 3 = 4x2; 4 = 2x2; 5 = 8x2.
+// block; 3 = 4x2; 4 = 2x2 (default when heights come in float4); 5 = 8x2;
+// 6 = runs along the axis of smaller step, two launches (bp_z0_runs_kernel).
 cudaError_t launch_backward_z0(const float* y, float* x, const float* angles, const Geom& g,
                                cudaStream_t stream) {
-  const bool vec4 = (g.Hx % 4 == 0) && (g.Hy % 4 == 0) &&
-                    ((reinterpret_cast<uintptr_t>(x) | reinterpret_cast<uintptr_t>(y)) & 15) == 0;
+  const bool vec4 = bp0_vec4(y, x, g);
   const int variant = kernel_variant(OP_BACKWARD_Z0);
   if (vec4 && variant != 1) {
     switch (variant) {
+      case 6: return launch_bp_z0_runs(y, x, angles, g, stream);
+      case 2: return launch_bp_z0_block<4, 4>(y, x, angles, g, stream);
       case 3: return launch_bp_z0_block<4, 2>(y, x, angles, g, stream);
-      case 4: return launch_bp_z0_block<2, 2>(y, x, angles, g, stream);
       case 5: return launch_bp_z0_block<8, 2>(y, x, angles, g, stream);
-      default: return launch_bp_z0_block<4, 4>(y, x, angles, g, stream);
+      default: return launch_bp_z0_block<2, 2>(y, x, angles, g, stream);
     }
   }
   const int R = vec4 ? 4 : 1;
   dim3 block(32, BP0_WARPS);
-  dim3 grid(ceil_div(g.H, 32 * R), ceil_div(g.SX, BP0_RUN), ceil_div(g.SY, BP0_WARPS));
+  dim3 grid(ceil_div(g.SX, BP0_RUN), ceil_div(g.SY, BP0_WARPS), ceil_div(g.H, 32 * R));
   if (vec4)
     bp_z0_kernel<4><<<grid, block, 0, stream>>>(y, x, angles, g);
   else

@@ -155,7 +155,8 @@ int vp_backward_z0(const float* y, int64_t y0, int64_t y1, int64_t y2, float* x,
   if (int s = make_geom(x, x0, x1, x2, y, y0, y1, y2, angles, n_angles, flags, &g, &empty))
     return s;
   if (empty) return VP_OK;
-  return finish(vp::launch_backward_z0(y, x, angles, g, (cudaStream_t)stream), 1);
+  return finish(vp::launch_backward_z0(y, x, angles, g, (cudaStream_t)stream),
+                vp::launches_backward_z0(y, x, g));
 }
 
 size_t vp_z2_workspace_bytes(int64_t x0, int64_t x1, int64_t x2, int64_t y0, int64_t y1,

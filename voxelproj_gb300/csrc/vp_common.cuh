@@ -74,12 +74,30 @@ __device__ __forceinline__ AngleConst angle_const(float phi, int trig) {
 //   coeff*(b+a) + 2*coeff*x    -a <= x < a
 //   1 - cd*(b-x)^2             a <= x < b
 //   1                          x >= b
+#ifndef VP_MID_FORM
+#define VP_MID_FORM 0
+#endif
+#ifndef VP_RIGHT_FORM
+#define VP_RIGHT_FORM 0
+#endif
 __device__ __forceinline__ float trap_cdf(float x, float a, float b, float coeff, float cd) {
   const float xl = x + b;
   const float xr = b - x;
   const float left = cd * xl * xl;
+#if VP_MID_FORM == 1
+  const float mid = __fmaf_rn(__fmul_rn(2.0f, coeff), x, __fmul_rn(coeff, __fadd_rn(b, a)));
+#elif VP_MID_FORM == 2
+  const float mid = __fmaf_rn(coeff, __fadd_rn(b, a), __fmul_rn(__fmul_rn(2.0f, coeff), x));
+#else
   const float mid = coeff * (b + a) + 2.0f * coeff * x;
+#endif
+#if VP_RIGHT_FORM == 1
+  const float right = __fmaf_rn(-__fmul_rn(cd, xr), xr, 1.0f);
+#elif VP_RIGHT_FORM == 2
+  const float right = __fsub_rn(1.0f, __fmul_rn(__fmul_rn(cd, xr), xr));
+#else
   const float right = 1.0f - cd * xr * xr;
+#endif
   float r = (x < b) ? right : 1.0f;
   r = (x < a) ? mid : r;
   r = (x < -a) ? left : r;

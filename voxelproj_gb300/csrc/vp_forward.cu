@@ -50,14 +50,14 @@ struct MinorRange {
 
 __device__ __forceinline__ MinorRange minor_range(int i, float cent_major, float sh_major,
                                                   float cent_minor, float inv_sh_minor,
-                                                  int n_minor, float pcent, float t_lo,
-                                                  float t_hi) {
+                                                  int min_lo, int min_hi, float pcent,
+                                                  float t_lo, float t_hi) {
   const float K = ((float)i - cent_major) * sh_major + pcent;
   const float u1 = (t_lo - K) * inv_sh_minor + cent_minor;
   const float u2 = (t_hi - K) * inv_sh_minor + cent_minor;
   MinorRange m;
-  m.lo = max(0, (int)ceilf(fminf(u1, u2)));
-  m.hi = min(n_minor - 1, (int)floorf(fmaxf(u1, u2)));
+  m.lo = max(min_lo, (int)ceilf(fminf(u1, u2)));
+  m.hi = min(min_hi, (int)floorf(fmaxf(u1, u2)));
   return m;
 }
 
@@ -71,6 +71,12 @@ __device__ __forceinline__ MinorRange minor_range(int i, float cent_major, float
 // accumulate the FP0_KW bins in registers.  A candidate's three bins sit at
 // run-relative offsets q-2, q-1, q (q = round(xp) - p0 + 1), dispatched with
 // a warp-uniform switch.
+//
+// Cache locality: every angle touches the whole volume, so a launch is
+// restricted to one slab of rows [y_lo, y_hi) of the volume (all launches add
+// into y), and heights are the slowest grid axis.  Concurrently running
+// blocks then share one slab x one 128-height chunk, a few tens of MB that
+// stay in L2 across all angles instead of being re-read from HBM per angle.
 // ---------------------------------------------------------------------------
 constexpr int FP0_KW = 4;
 constexpr int FP0_WARPS = 4;
@@ -90,22 +96,26 @@ __device__ __forceinline__ void scatter3(V (&acc)[KW], const float4& e, const V&
 template <int R>
 __global__ void __launch_bounds__(32 * FP0_WARPS)
     fp_z0_kernel(const float* __restrict__ x, float* __restrict__ y,
-                 const float* __restrict__ angles, Geom g, int a_base) {
+                 const float* __restrict__ angles, Geom g, int a_base, int y_lo, int y_hi,
+                 int accumulate) {
   using V = typename Vec<R>::T;
   __shared__ float4 cand[FP0_WARPS][32 * FP0_CAP];
 
   const int lane = threadIdx.x;
   const int w = threadIdx.y;
-  const int h = (blockIdx.x * 32 + lane) * R;
-  const int p0 = (blockIdx.y * FP0_WARPS + w) * FP0_KW;
-  const int a = a_base + blockIdx.z;
+  const int p0 = (blockIdx.x * FP0_WARPS + w) * FP0_KW;
+  const int a = a_base + blockIdx.y;
+  const int h = (blockIdx.z * 32 + lane) * R;
   if (p0 >= g.PX || a >= g.n_ang) return;  // warp-uniform
   const bool hv = h < g.H;
 
   const AngleConst k = angle_const(__ldg(angles + a), g.trig);
   const bool minor_x = fabsf(k.c) >= fabsf(k.s);
-  const int n_major = minor_x ? g.SY : g.SX;
-  const int n_minor = minor_x ? g.SX : g.SY;
+  // major lines [maj_lo, maj_hi), minor indices [min_lo, min_hi], within the slab
+  const int maj_lo = minor_x ? y_lo : 0;
+  const int maj_hi = minor_x ? y_hi : g.SX;
+  const int min_lo = minor_x ? 0 : y_lo;
+  const int min_hi = minor_x ? g.SX - 1 : y_hi - 1;
   const float cent_major = minor_x ? g.ycent : g.xcent;
   const float cent_minor = minor_x ? g.xcent : g.ycent;
   const float sh_major = minor_x ? k.s : k.c;
@@ -117,12 +127,12 @@ __global__ void __launch_bounds__(32 * FP0_WARPS)
 #pragma unroll
   for (int b = 0; b < FP0_KW; ++b) acc[b] = vzero<V>();
 
-  for (int i0 = 0; i0 < n_major; i0 += 32) {
+  for (int i0 = maj_lo; i0 < maj_hi; i0 += 32) {
     const int i = i0 + lane;
     int lo = 0, cnt = 0;
-    if (i < n_major) {
+    if (i < maj_hi) {
       const MinorRange mr = minor_range(i, cent_major, sh_major, cent_minor, inv_sh_minor,
-                                        n_minor, g.pcent, t_lo, t_hi);
+                                        min_lo, min_hi, g.pcent, t_lo, t_hi);
       lo = mr.lo;
       cnt = max(0, min(mr.hi - mr.lo + 1, FP0_CAP));
     }
@@ -175,7 +185,7 @@ __global__ void __launch_bounds__(32 * FP0_WARPS)
       const int p = p0 + b;
       if (p < g.PX) {
         V* py = reinterpret_cast<V*>(y + ((size_t)a * g.PX + p) * g.Hy + h);
-        store_out(py, acc[b], g.accumulate);
+        store_out(py, acc[b], accumulate);
       }
     }
   }
@@ -220,7 +230,7 @@ __global__ void __launch_bounds__(32 * FP2_WARPS)
   if (pv) {
     for (int i = 0; i < n_major; ++i) {
       const MinorRange mr = minor_range(i, cent_major, sh_major, cent_minor, inv_sh_minor,
-                                        n_minor, g.pcent, t_lo, t_hi);
+                                        0, n_minor - 1, g.pcent, t_lo, t_hi);
       for (int m = mr.lo; m <= mr.hi; ++m) {
         const int xi = minor_x ? m : i;
         const int yi = minor_x ? i : m;
@@ -252,8 +262,17 @@ constexpr int kMaxGridYZ = 65535;
 
 }  // namespace
 
+// Rows per slab: about 32 MB of one 128-height chunk of the volume.
+int fp0_slab_rows(const Geom& g) {
+  const long long bytes_per_row = (long long)g.SX * 128 * 4;
+  long long rows = (32ll << 20) / (bytes_per_row > 0 ? bytes_per_row : 1);
+  if (rows < 8) rows = 8;
+  return (int)(rows < g.SY ? rows : g.SY);
+}
+
 int launches_forward_z0(const Geom& g) {
-  return (int)ceil_div(g.n_ang, kMaxGridYZ);
+  const int rows = fp0_slab_rows(g);
+  return (int)(ceil_div(g.SY, rows) * ceil_div(g.n_ang, kMaxGridYZ));
 }
 
 int launches_forward_z2(const Geom& g) {
@@ -265,16 +284,26 @@ cudaError_t launch_forward_z0(const float* x, float* y, const float* angles, con
   const bool vec4 = (g.Hx % 4 == 0) && (g.Hy % 4 == 0) &&
                     ((reinterpret_cast<uintptr_t>(x) | reinterpret_cast<uintptr_t>(y)) & 15) == 0;
   const int R = vec4 ? 4 : 1;
+  const int rows = fp0_slab_rows(g);
   dim3 block(32, FP0_WARPS);
-  for (int a_base = 0; a_base < g.n_ang; a_base += kMaxGridYZ) {
-    const int na = g.n_ang - a_base < kMaxGridYZ ? g.n_ang - a_base : kMaxGridYZ;
-    dim3 grid(ceil_div(g.H, 32 * R), ceil_div(g.PX, FP0_KW * FP0_WARPS), na);
-    if (vec4)
-      fp_z0_kernel<4><<<grid, block, 0, stream>>>(x, y, angles, g, a_base);
-    else
-      fp_z0_kernel<1><<<grid, block, 0, stream>>>(x, y, angles, g, a_base);
-    const cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return e;
+  bool first = true;
+  for (int y_lo = 0; y_lo < g.SY; y_lo += rows) {
+    const int y_hi = y_lo + rows < g.SY ? y_lo + rows : g.SY;
+    // the first slab applies the caller's mode; later slabs add to it
+    const int accumulate = first ? g.accumulate : 1;
+    first = false;
+    for (int a_base = 0; a_base < g.n_ang; a_base += kMaxGridYZ) {
+      const int na = g.n_ang - a_base < kMaxGridYZ ? g.n_ang - a_base : kMaxGridYZ;
+      dim3 grid(ceil_div(g.PX, FP0_KW * FP0_WARPS), na, ceil_div(g.H, 32 * R));
+      if (vec4)
+        fp_z0_kernel<4><<<grid, block, 0, stream>>>(x, y, angles, g, a_base, y_lo, y_hi,
+                                                    accumulate);
+      else
+        fp_z0_kernel<1><<<grid, block, 0, stream>>>(x, y, angles, g, a_base, y_lo, y_hi,
+                                                    accumulate);
+      const cudaError_t e = cudaGetLastError();
+      if (e != cudaSuccess) return e;
+    }
   }
   return cudaSuccess;
 }

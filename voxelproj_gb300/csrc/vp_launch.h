@@ -37,6 +37,7 @@ cudaError_t backward_z2_transposed(const float* y, float* x, const float* angles
 // Kernel launches the forward launchers issue for a geometry (grids are
 // split past 65535 angle blocks).
 int launches_forward_z0(const Geom& g);
+int launches_backward_z0(const float* y, const float* x, const Geom& g);
 int launches_forward_z2(const Geom& g);
 
 }  // namespace vp

@@ -89,7 +89,12 @@ size_t z2_workspace_bytes(const Geom& g) {
 
 int launches_z2(const Geom& g, bool forward) {
   if (!z2_uses_transpose(g)) return forward ? launches_forward_z2(g) : 1;
-  return 2 + (forward ? launches_forward_z0(g) : 1);
+  // the transposed path runs the z_order 0 kernels on 16-byte aligned scratch
+  // with a height extent that is a multiple of 4
+  Geom g0 = g;
+  g0.H = g0.Hx = g0.Hy = (int)round4(g.H);
+  static const float aligned[4] = {};
+  return 2 + (forward ? launches_forward_z0(g0) : launches_backward_z0(aligned, aligned, g0));
 }
 
 // x (Hx, SY, SX) -> xt (SY, SX, Hp); yt = A xt; y (Hy, n, PX) += yt^T.

@@ -40,7 +40,8 @@ if str(ROOT) not in sys.path:
 
 METRIC = "GVU/s (voxel×angle) for A and Aᵀ at 512³/192 ang"
 UNIT = "GVU/s"
-# RTX 3060, README.md:58-59 (z_order 0, 512^3, 192 angles):
+# The reference's published timing (its README.md:58-59, RTX 3060, z_order 0,
+# 512^3, 192 angles, units taken as ms):
 # A 516 ms, A^T 397 ms -> 2 * 512^3 * 192 VU / 0.913 s.
 PUBLISHED_GVU_S = 2 * 512**3 * 192 / 0.913 / 1e9
 L2_BYTES = 129 * 2**20

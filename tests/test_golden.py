@@ -110,3 +110,8 @@ def test_kernels_match_reference(name):
     assert eb <= tol.REF_VS_REFERENCE
     assert e_ours64 <= tol.REF_VS_FP64
     assert e_ref <= e_ref64 + tol.REF_VS_FP64
+    if not name.startswith("many_angles"):
+        # same weights, same order of accumulation: the default A^T kernels
+        # reproduce the reference bit for bit (the 600-angle fixtures were
+        # recorded in two <= 512-angle chunks, which sums in another order)
+        np.testing.assert_array_equal(xo.cpu().numpy(), c["bwd"])

@@ -277,12 +277,21 @@ struct RunEntry {
   int4 meta;    // base bin of the window, direction (+1/-1), pattern, angle index
 };
 
+// Fast path for advance pattern PAT: loads the W = 3 + popcount(PAT) window
+// bins with no predicates (the table phase routed windows that leave the
+// detector to the generic path), then applies the four voxels' weights.
+// p points at the window's first bin for this lane's heights; stride is the
+// signed distance between consecutive window bins.
 template <int PAT>
-__device__ __forceinline__ void run_apply(float4 (&acc)[RUN], const float4 (&wv)[3],
-                                          const float4 (&win)[6]) {
+__device__ __forceinline__ void run_window(float4 (&acc)[RUN], const float4 (&wv)[3],
+                                           const float* p, ptrdiff_t stride) {
   constexpr int o1 = (PAT & 1);
   constexpr int o2 = o1 + ((PAT >> 1) & 1);
   constexpr int o3 = o2 + ((PAT >> 2) & 1);
+  constexpr int W = 3 + o3;
+  float4 win[W];
+#pragma unroll
+  for (int u = 0; u < W; ++u) win[u] = __ldg(reinterpret_cast<const float4*>(p + u * stride));
   const float ws[12] = {wv[0].x, wv[0].y, wv[0].z, wv[0].w, wv[1].x, wv[1].y,
                         wv[1].z, wv[1].w, wv[2].x, wv[2].y, wv[2].z, wv[2].w};
   constexpr int off[RUN] = {0, o1, o2, o3};
@@ -349,6 +358,10 @@ __global__ void __launch_bounds__(32 * BPR_WARPS)
         ok = ok && (d == 0 || d == 1);
         pattern |= (d == 1 ? 1 : 0) << m;
       }
+      // the fast path needs every window bin on the detector
+      const int base = bw[0].r - dir;
+      const int last = base + dir * (2 + __popc(pattern));
+      ok = ok && (unsigned)base < (unsigned)g.PX && (unsigned)last < (unsigned)g.PX;
       RunEntry e;
       float ws[12];
 #pragma unroll
@@ -362,34 +375,28 @@ __global__ void __launch_bounds__(32 * BPR_WARPS)
       e.w[1] = make_float4(ws[4], ws[5], ws[6], ws[7]);
       e.w[2] = make_float4(ws[8], ws[9], ws[10], ws[11]);
       e.r = make_int4(bw[0].r, bw[1].r, bw[2].r, bw[3].r);
-      e.meta = make_int4(bw[0].r - dir, dir, ok ? pattern : BPR_GENERIC, a);
+      e.meta = make_int4(base, dir, ok ? pattern : BPR_GENERIC, a);
       tab[w][slot] = e;
     }
     __syncwarp();
-    const float* yang_base = y + h;
+    const int hs = hv ? h : 0;  // idle lanes read valid memory and never store
     for (int j = 0; j < count; ++j) {
       const RunEntry& e = tab[w][j];
       const int4 meta = e.meta;
       const float4 wv[3] = {e.w[0], e.w[1], e.w[2]};
-      const float* yang = yang_base + (size_t)meta.w * yrow_stride;
+      const float* yang = y + (size_t)meta.w * yrow_stride + hs;
       if (meta.z != BPR_GENERIC) {
-        const int W = 3 + __popc(meta.z);
-        float4 win[6];
-#pragma unroll
-        for (int u = 0; u < 6; ++u) {
-          const int bin = meta.x + meta.y * u;
-          win[u] = ld_or_zero<float4>(yang + (ptrdiff_t)bin * g.Hy,
-                                      hv && u < W && (unsigned)bin < (unsigned)g.PX);
-        }
+        const float* p = yang + (ptrdiff_t)meta.x * g.Hy;
+        const ptrdiff_t stride = (ptrdiff_t)meta.y * g.Hy;
         switch (meta.z) {
-          case 0: run_apply<0>(acc, wv, win); break;
-          case 1: run_apply<1>(acc, wv, win); break;
-          case 2: run_apply<2>(acc, wv, win); break;
-          case 3: run_apply<3>(acc, wv, win); break;
-          case 4: run_apply<4>(acc, wv, win); break;
-          case 5: run_apply<5>(acc, wv, win); break;
-          case 6: run_apply<6>(acc, wv, win); break;
-          default: run_apply<7>(acc, wv, win); break;
+          case 0: run_window<0>(acc, wv, p, stride); break;
+          case 1: run_window<1>(acc, wv, p, stride); break;
+          case 2: run_window<2>(acc, wv, p, stride); break;
+          case 3: run_window<3>(acc, wv, p, stride); break;
+          case 4: run_window<4>(acc, wv, p, stride); break;
+          case 5: run_window<5>(acc, wv, p, stride); break;
+          case 6: run_window<6>(acc, wv, p, stride); break;
+          default: run_window<7>(acc, wv, p, stride); break;
         }
       } else {
         const int rr[RUN] = {e.r.x, e.r.y, e.r.z, e.r.w};
@@ -401,7 +408,7 @@ __global__ void __launch_bounds__(32 * BPR_WARPS)
           for (int kk = 0; kk < 3; ++kk) {
             const int bin = rr[m] + meta.y * (kk - 1);
             const float4 v = ld_or_zero<float4>(yang + (ptrdiff_t)bin * g.Hy,
-                                                hv && (unsigned)bin < (unsigned)g.PX);
+                                                (unsigned)bin < (unsigned)g.PX);
             acc[m] = f4_fma(ws[3 * m + kk], v, acc[m]);
           }
         }

@@ -19,8 +19,8 @@ std::atomic<uint64_t> g_launches{0};
 std::atomic<int> g_variant[vp::OP_COUNT] = {};
 
 constexpr int64_t kMaxDim = (int64_t)1 << 30;
-// fp_z0 packs the voxel index (yi*SX + xi) with 3 tag bits into an int.
-constexpr int64_t kMaxVoxelsPerSlice = (int64_t)1 << 28;
+// fp_z0 packs the voxel index (yi*SX + xi) with 4 tag bits into an int.
+constexpr int64_t kMaxVoxelsPerSlice = (int64_t)1 << 27;
 
 int check_flags(int flags) { return (flags & ~VP_FLAG_TRIG_PRECISE) ? VP_ERR_BAD_FLAGS : VP_OK; }
 

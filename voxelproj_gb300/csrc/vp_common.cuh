@@ -74,30 +74,12 @@ __device__ __forceinline__ AngleConst angle_const(float phi, int trig) {
 //   coeff*(b+a) + 2*coeff*x    -a <= x < a
 //   1 - cd*(b-x)^2             a <= x < b
 //   1                          x >= b
-#ifndef VP_MID_FORM
-#define VP_MID_FORM 0
-#endif
-#ifndef VP_RIGHT_FORM
-#define VP_RIGHT_FORM 0
-#endif
 __device__ __forceinline__ float trap_cdf(float x, float a, float b, float coeff, float cd) {
-  const float xl = x + b;
-  const float xr = b - x;
-  const float left = cd * xl * xl;
-#if VP_MID_FORM == 1
-  const float mid = __fmaf_rn(__fmul_rn(2.0f, coeff), x, __fmul_rn(coeff, __fadd_rn(b, a)));
-#elif VP_MID_FORM == 2
+  const float xl = __fadd_rn(x, b);
+  const float xr = __fsub_rn(b, x);
+  const float left = __fmul_rn(__fmul_rn(cd, xl), xl);
   const float mid = __fmaf_rn(coeff, __fadd_rn(b, a), __fmul_rn(__fmul_rn(2.0f, coeff), x));
-#else
-  const float mid = coeff * (b + a) + 2.0f * coeff * x;
-#endif
-#if VP_RIGHT_FORM == 1
   const float right = __fmaf_rn(-__fmul_rn(cd, xr), xr, 1.0f);
-#elif VP_RIGHT_FORM == 2
-  const float right = __fsub_rn(1.0f, __fmul_rn(__fmul_rn(cd, xr), xr));
-#else
-  const float right = 1.0f - cd * xr * xr;
-#endif
   float r = (x < b) ? right : 1.0f;
   r = (x < a) ? mid : r;
   r = (x < -a) ? left : r;
@@ -105,20 +87,13 @@ __device__ __forceinline__ float trap_cdf(float x, float a, float b, float coeff
   return r;
 }
 
-// Detector coordinate of a voxel with centred coordinates (relx, rely), in
-// one fixed rounding order so every kernel (and both directions) computes
-// bit-identical weights.  VP_XP_FORM selects which product is fused.
-#ifndef VP_XP_FORM
-#define VP_XP_FORM 0
-#endif
+// Detector coordinate of a voxel with centred coordinates (relx, rely), with a
+// fixed rounding order: xp = fma(relx, c, rely*s) + pcent.  Every kernel and
+// both directions use it, so A and A^T carry bit-identical weights.  With the
+// CDF below and TRIG_REF, A^T reproduces the reference's kernels bit for bit
+// (checked against its recorded outputs).
 __device__ __forceinline__ float det_coord(float relx, float rely, float c, float s, float pcent) {
-#if VP_XP_FORM == 1
   return __fadd_rn(__fmaf_rn(relx, c, __fmul_rn(rely, s)), pcent);
-#elif VP_XP_FORM == 2
-  return __fadd_rn(__fmaf_rn(rely, s, __fmul_rn(relx, c)), pcent);
-#else
-  return relx * c + rely * s + pcent;
-#endif
 }
 
 // Weights of bins r-1, r, r+1 for a voxel projecting to xp

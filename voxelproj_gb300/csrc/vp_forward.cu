@@ -78,11 +78,15 @@ __device__ __forceinline__ MinorRange minor_range(int i, float cent_major, float
 // blocks then share one slab x one 128-height chunk, a few tens of MB that
 // stay in L2 across all angles instead of being re-read from HBM per angle.
 // ---------------------------------------------------------------------------
-constexpr int FP0_KW = 4;
+constexpr int FP0_KW = 8;
 constexpr int FP0_WARPS = 4;
-constexpr int FP0_CAP = 10;  // >= max candidates per major line: (KW + 2b)/sqrt(1/2) + 1
+// >= max candidates per major line: floor((KW + 2b + margin) / sqrt(1/2)) + 1
+constexpr int FP0_CAP = 15;
+constexpr int FP0_QBITS = 4;  // q in [0, KW + 1]
+constexpr int FP0_UNROLL = 4; // candidates whose loads are in flight together
 
-static_assert(FP0_KW == 4, "the dispatch switch below lists q = 0..KW+1");
+static_assert(FP0_KW + 1 < (1 << FP0_QBITS), "q must fit its bits");
+static_assert(FP0_KW == 8, "the dispatch switch below lists q = 0..KW+1");
 
 // Adds a candidate's weights to the run's accumulators: bin q-2 gets w0, q-1
 // gets w1, q gets w2 (run-relative); bins outside [0, KW) are dropped.
@@ -157,23 +161,37 @@ __global__ void __launch_bounds__(32 * FP0_WARPS)
         e = make_float4(0.f, 0.f, 0.f, 0.f);
       }
       const int vox = yi * g.SX + xi;
-      e.w = __int_as_float((vox << 3) | q);
+      e.w = __int_as_float((vox << FP0_QBITS) | q);
       cand[w][start + t] = e;
     }
     __syncwarp();
-    for (int c = 0; c < total; ++c) {
-      const float4 e = cand[w][c];
-      const int pk = __float_as_int(e.w);
-      const int vox = pk >> 3;
-      const int q = pk & 7;
-      const V xv = ld_or_zero<V>(x + (size_t)vox * g.Hx + h, hv);
-      switch (q) {
-        case 0: scatter3<FP0_KW, 0>(acc, e, xv); break;
-        case 1: scatter3<FP0_KW, 1>(acc, e, xv); break;
-        case 2: scatter3<FP0_KW, 2>(acc, e, xv); break;
-        case 3: scatter3<FP0_KW, 3>(acc, e, xv); break;
-        case 4: scatter3<FP0_KW, 4>(acc, e, xv); break;
-        default: scatter3<FP0_KW, 5>(acc, e, xv); break;
+    // Stream the list FP0_UNROLL candidates at a time so their loads overlap;
+    // idle lanes read row 0 (always valid) and never store.
+    const int hs = hv ? h : 0;
+    for (int c0 = 0; c0 < total; c0 += FP0_UNROLL) {
+      float4 e[FP0_UNROLL];
+      V xv[FP0_UNROLL];
+#pragma unroll
+      for (int u = 0; u < FP0_UNROLL; ++u) {
+        e[u] = (c0 + u < total) ? cand[w][c0 + u] : make_float4(0.f, 0.f, 0.f, 0.f);
+        const int vox = __float_as_int(e[u].w) >> FP0_QBITS;
+        xv[u] = __ldg(reinterpret_cast<const V*>(x + (size_t)vox * g.Hx + hs));
+      }
+#pragma unroll
+      for (int u = 0; u < FP0_UNROLL; ++u) {
+        if (c0 + u >= total) break;  // padding slots (warp-uniform)
+        switch (__float_as_int(e[u].w) & ((1 << FP0_QBITS) - 1)) {
+          case 0: scatter3<FP0_KW, 0>(acc, e[u], xv[u]); break;
+          case 1: scatter3<FP0_KW, 1>(acc, e[u], xv[u]); break;
+          case 2: scatter3<FP0_KW, 2>(acc, e[u], xv[u]); break;
+          case 3: scatter3<FP0_KW, 3>(acc, e[u], xv[u]); break;
+          case 4: scatter3<FP0_KW, 4>(acc, e[u], xv[u]); break;
+          case 5: scatter3<FP0_KW, 5>(acc, e[u], xv[u]); break;
+          case 6: scatter3<FP0_KW, 6>(acc, e[u], xv[u]); break;
+          case 7: scatter3<FP0_KW, 7>(acc, e[u], xv[u]); break;
+          case 8: scatter3<FP0_KW, 8>(acc, e[u], xv[u]); break;
+          default: scatter3<FP0_KW, 9>(acc, e[u], xv[u]); break;
+        }
       }
     }
     __syncwarp();

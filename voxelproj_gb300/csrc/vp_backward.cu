@@ -556,23 +556,26 @@ bool bp0_vec4(const float* y, const float* x, const Geom& g) {
 }
 
 int launches_backward_z0(const float* y, const float* x, const Geom& g) {
-  return (bp0_vec4(y, x, g) && kernel_variant(OP_BACKWARD_Z0) == 6) ? 2 : 1;
+  const int v = kernel_variant(OP_BACKWARD_Z0);
+  return (bp0_vec4(y, x, g) && (v == 0 || v == 6)) ? 2 : 1;
 }
 
 // Variants: 1 = one voxel run per warp (bp_z0_kernel); 2 = 4x4 register
-// block; 3 = 4x2; 4 = 2x2 (default when heights come in float4); 5 = 8x2;
-// 6 = runs along the axis of smaller step, two launches (bp_z0_runs_kernel).
+// block; 3 = 4x2; 4 = 2x2 (accumulates in the reference's order, so its
+// results equal the reference's bit for bit); 5 = 8x2; 6 = runs along the
+// axis of smaller step, two launches (bp_z0_runs_kernel; the default when
+// heights come in float4, as the fastest).
 cudaError_t launch_backward_z0(const float* y, float* x, const float* angles, const Geom& g,
                                cudaStream_t stream) {
   const bool vec4 = bp0_vec4(y, x, g);
   const int variant = kernel_variant(OP_BACKWARD_Z0);
   if (vec4 && variant != 1) {
     switch (variant) {
-      case 6: return launch_bp_z0_runs(y, x, angles, g, stream);
       case 2: return launch_bp_z0_block<4, 4>(y, x, angles, g, stream);
       case 3: return launch_bp_z0_block<4, 2>(y, x, angles, g, stream);
+      case 4: return launch_bp_z0_block<2, 2>(y, x, angles, g, stream);
       case 5: return launch_bp_z0_block<8, 2>(y, x, angles, g, stream);
-      default: return launch_bp_z0_block<2, 2>(y, x, angles, g, stream);
+      default: return launch_bp_z0_runs(y, x, angles, g, stream);
     }
   }
   const int R = vec4 ? 4 : 1;

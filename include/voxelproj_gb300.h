@@ -61,6 +61,7 @@ extern "C" {
 #define VP_ERR_BAD_FLAGS 5      /* unknown bit in `flags` */
 #define VP_ERR_BAD_Z_ORDER 6    /* z_order other than 0 or 2 */
 #define VP_ERR_WORKSPACE 7      /* workspace smaller than vp_z2_workspace_bytes() */
+#define VP_ERR_SCRATCH_LIMIT 8  /* problem too large for vp_forward_z2_noalloc's array */
 
 /* Flags. */
 #define VP_FLAG_TRIG_PRECISE 1  /* accurate sincosf / IEEE division for the per-angle
@@ -131,6 +132,22 @@ VP_API int vp_backward_z2_ws(const float* y, int64_t y0, int64_t y1, int64_t y2,
                              float* x, int64_t x0, int64_t x1, int64_t x2,
                              const float* angles, int64_t n_angles, int flags,
                              void* workspace, size_t workspace_bytes, void* stream);
+
+/* y += A x, z_order 2, allocating nothing: for callers that may not allocate
+ * device memory while they run (code that fixes its memory at start-up,
+ * hosts whose own allocator owns the device).  Same arguments and results as
+ * vp_forward_z2, but its scratch is an array of VP_NOALLOC_SCRATCH_BYTES
+ * (64 MiB) compiled into the library, held by every GPU that loads the
+ * library until the process exits.  Problems needing more scratch than that
+ * (vp_z2_workspace_bytes) return VP_ERR_SCRATCH_LIMIT and leave y unchanged.
+ * The first call on a device looks up the array's address (make it before
+ * any stream capture).  All calls share the array: calls that overlap on the
+ * GPU race and must be ordered by the caller.  No counterpart in the
+ * reference. */
+#define VP_NOALLOC_SCRATCH_BYTES ((size_t)64 << 20)
+VP_API int vp_forward_z2_noalloc(const float* x, int64_t x0, int64_t x1, int64_t x2,
+                                 float* y, int64_t y0, int64_t y1, int64_t y2,
+                                 const float* angles, int64_t n_angles, int flags, void* stream);
 
 /* z_order dispatch, as voxelproj.wrappers.forward/backward select a kernel by
  * z_order (voxelproj/wrappers.py:44-47, :92-95); dims as for the

@@ -41,7 +41,7 @@ def test_binding_covers_header():
 
 
 def test_status_strings():
-    for code in range(0, 8):
+    for code in range(0, 9):
         assert _lib.LIB.vp_error_string(code)
     assert b"unknown" in _lib.LIB.vp_error_string(99)
 

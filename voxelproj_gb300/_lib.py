@@ -20,6 +20,8 @@ VP_ERR_CUDA = 4
 VP_ERR_BAD_FLAGS = 5
 VP_ERR_BAD_Z_ORDER = 6
 VP_ERR_WORKSPACE = 7
+VP_ERR_SCRATCH_LIMIT = 8
+VP_NOALLOC_SCRATCH_BYTES = 64 << 20
 
 VP_FLAG_TRIG_PRECISE = 1
 
@@ -44,6 +46,8 @@ SIGNATURES = {
                               ctypes.c_size_t, _P]),
     "vp_backward_z2_ws": (_I, [_P, _I64, _I64, _I64, _P, _I64, _I64, _I64, _P, _I64, _I, _P,
                                ctypes.c_size_t, _P]),
+    "vp_forward_z2_noalloc": (_I, [_P, _I64, _I64, _I64, _P, _I64, _I64, _I64, _P, _I64, _I,
+                                   _P]),
     "vp_forward": (_I, [_P, _P, _P, _P, _P, _I64, _I, _I, _P]),
     "vp_backward": (_I, [_P, _P, _P, _P, _P, _I64, _I, _I, _P]),
 }

@@ -127,6 +127,9 @@ const char* vp_error_string(int status) {
     case VP_ERR_BAD_FLAGS: return "unknown flag bits";
     case VP_ERR_BAD_Z_ORDER: return "z_order must be 0 or 2";
     case VP_ERR_WORKSPACE: return "workspace smaller than vp_z2_workspace_bytes()";
+    case VP_ERR_SCRATCH_LIMIT:
+      return "problem needs more scratch than the library's static array holds "
+             "(VP_NOALLOC_SCRATCH_BYTES); use vp_forward_z2 or vp_forward_z2_ws";
     default: return "unknown status";
   }
 }
@@ -269,3 +272,74 @@ int vp_backward(const float* y, const int64_t y_dims[3], float* x, const int64_t
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Forward projection in z_order 2 without any device allocation.
+//
+// Some callers may not allocate device memory once they are running: code
+// that must not allocate after start-up (a real-time acquisition loop, a
+// service with a fixed memory plan), or a host framework that owns all device
+// memory through its own allocator and forbids outside cudaMalloc.
+// vp_forward_z2 needs scratch for its transposed path and takes it from a
+// pool; this entry point instead uses a fixed array compiled into the library.
+//
+// The array, g_noalloc_scratch, is a file-scope __device__ array of
+// VP_NOALLOC_SCRATCH_BYTES (64 MiB).  Every GPU that loads this library's
+// code holds it until the process exits.  Host code cannot use the symbol
+// itself as a device address (on the host it names a shadow object), so the
+// first call on each device looks up the array's device address with
+// cudaGetSymbolAddress, with that device current, and caches it.  Make that
+// first call before any stream capture.
+//
+// All calls on a device share the array, and it keeps whatever the previous
+// call left.  Nothing in this path reads scratch before writing it: the
+// input is transposed into the array, the projector stores (not adds) its
+// result there, and only those values are copied back.  Pad heights up to a
+// multiple of 4 carry leftovers, but they are never copied out.  Two calls
+// that overlap on the GPU (different streams, no ordering between them) race
+// on the array and corrupt each other's results.
+// ---------------------------------------------------------------------------
+namespace {
+
+constexpr size_t kNoallocScratchFloats = VP_NOALLOC_SCRATCH_BYTES / sizeof(float);
+static __device__ __align__(256) float g_noalloc_scratch[kNoallocScratchFloats];
+
+std::mutex g_noalloc_mutex;
+float* g_noalloc_addr[kMaxDevices] = {};
+
+// Device address of g_noalloc_scratch on the current device (looked up once).
+cudaError_t noalloc_scratch(float** out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  if (g_noalloc_addr[dev] == nullptr) {
+    void* ptr = nullptr;
+    e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+    if (e != cudaSuccess) return e;
+    g_noalloc_addr[dev] = static_cast<float*>(ptr);
+  }
+  *out = g_noalloc_addr[dev];
+  return cudaSuccess;
+}
+
+}  // namespace
+
+extern "C" int vp_forward_z2_noalloc(const float* x, int64_t x0, int64_t x1, int64_t x2, float* y,
+                                     int64_t y0, int64_t y1, int64_t y2, const float* angles,
+                                     int64_t n_angles, int flags, void* stream) {
+  vp::Geom g;
+  bool empty = false;
+  if (int s = make_geom(x, x1, x2, x0, y, y1, y2, y0, angles, n_angles, flags, &g, &empty))
+    return s;
+  if (empty) return VP_OK;
+  const size_t need = vp::z2_workspace_bytes(g);
+  if (need > VP_NOALLOC_SCRATCH_BYTES) return VP_ERR_SCRATCH_LIMIT;
+  float* scratch = nullptr;
+  if (need > 0) {
+    const cudaError_t e = noalloc_scratch(&scratch);
+    if (e != cudaSuccess) return finish(e, 0);
+  }
+  return run_z2(true, x, y, angles, g, scratch, VP_NOALLOC_SCRATCH_BYTES, (cudaStream_t)stream);
+}

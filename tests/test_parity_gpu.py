@@ -183,3 +183,29 @@ def test_backward_variants_store_mode_via_z2(variant):
         _lib.LIB.vp_set_kernel_variant(1, 0)
     np.testing.assert_array_equal(outs[0], outs[1])
     assert rel_err(outs[0] - x0, oracle.backward(y, ang, SY, SX, 2)) <= tol.ref_vs_fp64(PX)
+
+
+@pytest.mark.parametrize("variant", [1, 2, 3, 4])
+@pytest.mark.parametrize("geom", [(23, 37, 132, 61, 50, "wide"), (9, 6, 8, 40, 11, "axes"),
+                                  (70, 64, 256, 96, 90, "rand")],
+                         ids=lambda g: "x".join(map(str, g[:5])) + g[5])
+def test_forward_variants(variant, geom):
+    """Every kernel variant of the z_order 0 forward against the oracle:
+    bins per warp 4 / 8, warps of a block on neighbouring bins / angles, angle
+    counts that are not multiples of the group, degenerate angles."""
+    from voxelproj_gb300 import _lib
+
+    SY, SX, H, n, PX, kind = geom
+    ang = angle_set(kind, n, 98)
+    x = seeded((SY, SX, H), 33)
+    y0 = seeded((n, PX, H), 34)
+    _lib.LIB.vp_set_kernel_variant(0, variant)
+    try:
+        yo = torch.tensor(y0, device="cuda")
+        vp._CU.forward_z0(torch.tensor(x, device="cuda"), yo, torch.tensor(ang, device="cuda"))
+        torch.cuda.synchronize()
+    finally:
+        _lib.LIB.vp_set_kernel_variant(0, 0)
+    err = rel_err(yo.cpu().numpy() - y0, oracle.forward(x, ang, PX, 0))
+    print(f"\n[fwd variant {variant}] {geom}: A {err:.3e}")
+    assert err <= tol.ref_vs_fp64(max(SY, SX, PX))

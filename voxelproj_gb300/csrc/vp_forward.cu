@@ -63,30 +63,36 @@ __device__ __forceinline__ MinorRange minor_range(int i, float cent_major, float
 
 // ---------------------------------------------------------------------------
 // z_order 0: x (SY, SX, H), y (n_ang, PX, H); heights contiguous.
-// A warp owns angle a, FP0_KW consecutive bins and 32*R heights (lane <->
+// A warp owns angle a, KW consecutive bins and 32*R heights (lane <->
 // heights).  The voxels gathered are warp-uniform, so the warp enumerates
 // them cooperatively: lane j takes major line i0+j, computes its candidate
 // voxels and their bin weights into a per-warp shared list (offsets from a
-// warp prefix sum), then all lanes stream the list with broadcast reads and
-// accumulate the FP0_KW bins in registers.  A candidate's three bins sit at
-// run-relative offsets q-2, q-1, q (q = round(xp) - p0 + 1), dispatched with
-// a warp-uniform switch.
+// warp prefix sum), then all lanes stream the list with broadcast reads,
+// FP0_UNROLL candidates at a time so their loads overlap, and accumulate
+// the KW bins in registers.  A candidate's three bins sit at run-relative
+// offsets q-2, q-1, q (q = round(xp) - p0 + 1), dispatched with a
+// warp-uniform switch.
 //
 // Cache locality: every angle touches the whole volume, so a launch is
 // restricted to one slab of rows [y_lo, y_hi) of the volume (all launches add
 // into y), and heights are the slowest grid axis.  Concurrently running
 // blocks then share one slab x one 128-height chunk, a few tens of MB that
 // stay in L2 across all angles instead of being re-read from HBM per angle.
+// With AGROUP the four warps of a block take four consecutive angles of the
+// same bins: their voxel strips largely coincide, so one warp's loads are L1
+// hits for the others.
 // ---------------------------------------------------------------------------
-constexpr int FP0_KW = 8;
 constexpr int FP0_WARPS = 4;
-// >= max candidates per major line: floor((KW + 2b + margin) / sqrt(1/2)) + 1
-constexpr int FP0_CAP = 15;
-constexpr int FP0_QBITS = 4;  // q in [0, KW + 1]
-constexpr int FP0_UNROLL = 4; // candidates whose loads are in flight together
+constexpr int FP0_QBITS = 4;   // q in [0, KW + 1]
+constexpr int FP0_UNROLL = 4;  // candidates whose loads are in flight together
 
-static_assert(FP0_KW + 1 < (1 << FP0_QBITS), "q must fit its bits");
-static_assert(FP0_KW == 8, "the dispatch switch below lists q = 0..KW+1");
+// >= max candidates per major line: floor((KW + 2b + margin) / sqrt(1/2)) + 1
+template <int KW>
+struct Fp0Cap {
+  static constexpr int value = KW == 4 ? 10 : 15;
+  static_assert(KW == 4 || KW == 8, "bins per warp: 4 or 8");
+  static_assert(KW + 1 < (1 << FP0_QBITS), "q must fit its bits");
+};
 
 // Adds a candidate's weights to the run's accumulators: bin q-2 gets w0, q-1
 // gets w1, q gets w2 (run-relative); bins outside [0, KW) are dropped.
@@ -97,18 +103,33 @@ __device__ __forceinline__ void scatter3(V (&acc)[KW], const float4& e, const V&
   if constexpr (Q < KW) acc[Q] = f4_fma(e.z, xv, acc[Q]);
 }
 
-template <int R>
+template <int KW, typename V>
+__device__ __forceinline__ void scatter_q(V (&acc)[KW], const float4& e, const V& xv, int q) {
+#define VP_Q_CASE(Q)                                            \
+  case Q:                                                       \
+    if constexpr (Q <= KW + 1) scatter3<KW, Q>(acc, e, xv);     \
+    break;
+  switch (q) {
+    VP_Q_CASE(0) VP_Q_CASE(1) VP_Q_CASE(2) VP_Q_CASE(3) VP_Q_CASE(4)
+    VP_Q_CASE(5) VP_Q_CASE(6) VP_Q_CASE(7) VP_Q_CASE(8) VP_Q_CASE(9)
+    default: break;
+  }
+#undef VP_Q_CASE
+}
+
+template <int R, int KW, bool AGROUP>
 __global__ void __launch_bounds__(32 * FP0_WARPS)
     fp_z0_kernel(const float* __restrict__ x, float* __restrict__ y,
                  const float* __restrict__ angles, Geom g, int a_base, int y_lo, int y_hi,
                  int accumulate) {
   using V = typename Vec<R>::T;
-  __shared__ float4 cand[FP0_WARPS][32 * FP0_CAP];
+  constexpr int CAP = Fp0Cap<KW>::value;
+  __shared__ float4 cand[FP0_WARPS][32 * CAP];
 
   const int lane = threadIdx.x;
   const int w = threadIdx.y;
-  const int p0 = (blockIdx.x * FP0_WARPS + w) * FP0_KW;
-  const int a = a_base + blockIdx.y;
+  const int p0 = (AGROUP ? blockIdx.x : blockIdx.x * FP0_WARPS + w) * KW;
+  const int a = a_base + (AGROUP ? blockIdx.y * FP0_WARPS + w : blockIdx.y);
   const int h = (blockIdx.z * 32 + lane) * R;
   if (p0 >= g.PX || a >= g.n_ang) return;  // warp-uniform
   const bool hv = h < g.H;
@@ -125,11 +146,12 @@ __global__ void __launch_bounds__(32 * FP0_WARPS)
   const float sh_major = minor_x ? k.s : k.c;
   const float inv_sh_minor = 1.0f / (minor_x ? k.c : k.s);
   const float t_lo = (float)p0 - 0.5f - k.b - kWindowMargin;
-  const float t_hi = (float)(p0 + FP0_KW) - 0.5f + k.b + kWindowMargin;
+  const float t_hi = (float)(p0 + KW) - 0.5f + k.b + kWindowMargin;
 
-  V acc[FP0_KW];
+  V acc[KW];
 #pragma unroll
-  for (int b = 0; b < FP0_KW; ++b) acc[b] = vzero<V>();
+  for (int b = 0; b < KW; ++b) acc[b] = vzero<V>();
+  const int hs = hv ? h : 0;  // idle lanes read row 0 (always valid) and never store
 
   for (int i0 = maj_lo; i0 < maj_hi; i0 += 32) {
     const int i = i0 + lane;
@@ -138,7 +160,7 @@ __global__ void __launch_bounds__(32 * FP0_WARPS)
       const MinorRange mr = minor_range(i, cent_major, sh_major, cent_minor, inv_sh_minor,
                                         min_lo, min_hi, g.pcent, t_lo, t_hi);
       lo = mr.lo;
-      cnt = max(0, min(mr.hi - mr.lo + 1, FP0_CAP));
+      cnt = max(0, min(mr.hi - mr.lo + 1, CAP));
     }
     int incl = cnt;
 #pragma unroll
@@ -156,7 +178,7 @@ __global__ void __launch_bounds__(32 * FP0_WARPS)
           voxel_weights((float)xi - g.xcent, (float)yi - g.ycent, k, g.pcent, g.trig);
       int q = bw.r - p0 + 1;
       float4 e = make_float4(bw.w0, bw.w1, bw.w2, 0.0f);
-      if (q < 0 || q > FP0_KW + 1) {
+      if (q < 0 || q > KW + 1) {
         q = 0;
         e = make_float4(0.f, 0.f, 0.f, 0.f);
       }
@@ -165,9 +187,6 @@ __global__ void __launch_bounds__(32 * FP0_WARPS)
       cand[w][start + t] = e;
     }
     __syncwarp();
-    // Stream the list FP0_UNROLL candidates at a time so their loads overlap;
-    // idle lanes read row 0 (always valid) and never store.
-    const int hs = hv ? h : 0;
     for (int c0 = 0; c0 < total; c0 += FP0_UNROLL) {
       float4 e[FP0_UNROLL];
       V xv[FP0_UNROLL];
@@ -180,18 +199,7 @@ __global__ void __launch_bounds__(32 * FP0_WARPS)
 #pragma unroll
       for (int u = 0; u < FP0_UNROLL; ++u) {
         if (c0 + u >= total) break;  // padding slots (warp-uniform)
-        switch (__float_as_int(e[u].w) & ((1 << FP0_QBITS) - 1)) {
-          case 0: scatter3<FP0_KW, 0>(acc, e[u], xv[u]); break;
-          case 1: scatter3<FP0_KW, 1>(acc, e[u], xv[u]); break;
-          case 2: scatter3<FP0_KW, 2>(acc, e[u], xv[u]); break;
-          case 3: scatter3<FP0_KW, 3>(acc, e[u], xv[u]); break;
-          case 4: scatter3<FP0_KW, 4>(acc, e[u], xv[u]); break;
-          case 5: scatter3<FP0_KW, 5>(acc, e[u], xv[u]); break;
-          case 6: scatter3<FP0_KW, 6>(acc, e[u], xv[u]); break;
-          case 7: scatter3<FP0_KW, 7>(acc, e[u], xv[u]); break;
-          case 8: scatter3<FP0_KW, 8>(acc, e[u], xv[u]); break;
-          default: scatter3<FP0_KW, 9>(acc, e[u], xv[u]); break;
-        }
+        scatter_q<KW>(acc, e[u], xv[u], __float_as_int(e[u].w) & ((1 << FP0_QBITS) - 1));
       }
     }
     __syncwarp();
@@ -199,7 +207,7 @@ __global__ void __launch_bounds__(32 * FP0_WARPS)
 
   if (hv) {
 #pragma unroll
-    for (int b = 0; b < FP0_KW; ++b) {
+    for (int b = 0; b < KW; ++b) {
       const int p = p0 + b;
       if (p < g.PX) {
         V* py = reinterpret_cast<V*>(y + ((size_t)a * g.PX + p) * g.Hy + h);
@@ -290,40 +298,63 @@ int fp0_slab_rows(const Geom& g) {
 
 int launches_forward_z0(const Geom& g) {
   const int rows = fp0_slab_rows(g);
-  return (int)(ceil_div(g.SY, rows) * ceil_div(g.n_ang, kMaxGridYZ));
+  const int v = kernel_variant(OP_FORWARD_Z0);
+  const long long per = (v == 1 || v == 2) ? kMaxGridYZ : (long long)kMaxGridYZ * FP0_WARPS;
+  return (int)(ceil_div(g.SY, rows) * ceil_div(g.n_ang, per));
 }
 
 int launches_forward_z2(const Geom& g) {
   return (int)ceil_div(g.n_ang, (long long)kMaxGridYZ * FP2_WARPS);
 }
 
-cudaError_t launch_forward_z0(const float* x, float* y, const float* angles, const Geom& g,
-                              cudaStream_t stream) {
-  const bool vec4 = (g.Hx % 4 == 0) && (g.Hy % 4 == 0) &&
-                    ((reinterpret_cast<uintptr_t>(x) | reinterpret_cast<uintptr_t>(y)) & 15) == 0;
-  const int R = vec4 ? 4 : 1;
+template <int R, int KW, bool AGROUP>
+cudaError_t launch_fp_z0(const float* x, float* y, const float* angles, const Geom& g,
+                         cudaStream_t stream) {
   const int rows = fp0_slab_rows(g);
   dim3 block(32, FP0_WARPS);
   bool first = true;
+  const long long angles_per_launch = AGROUP ? (long long)kMaxGridYZ * FP0_WARPS : kMaxGridYZ;
   for (int y_lo = 0; y_lo < g.SY; y_lo += rows) {
     const int y_hi = y_lo + rows < g.SY ? y_lo + rows : g.SY;
     // the first slab applies the caller's mode; later slabs add to it
     const int accumulate = first ? g.accumulate : 1;
     first = false;
-    for (int a_base = 0; a_base < g.n_ang; a_base += kMaxGridYZ) {
-      const int na = g.n_ang - a_base < kMaxGridYZ ? g.n_ang - a_base : kMaxGridYZ;
-      dim3 grid(ceil_div(g.PX, FP0_KW * FP0_WARPS), na, ceil_div(g.H, 32 * R));
-      if (vec4)
-        fp_z0_kernel<4><<<grid, block, 0, stream>>>(x, y, angles, g, a_base, y_lo, y_hi,
-                                                    accumulate);
-      else
-        fp_z0_kernel<1><<<grid, block, 0, stream>>>(x, y, angles, g, a_base, y_lo, y_hi,
-                                                    accumulate);
+    for (long long a_base = 0; a_base < g.n_ang; a_base += angles_per_launch) {
+      const long long na = g.n_ang - a_base < angles_per_launch ? g.n_ang - a_base
+                                                                 : angles_per_launch;
+      const unsigned gx = AGROUP ? ceil_div(g.PX, KW) : ceil_div(g.PX, KW * FP0_WARPS);
+      const unsigned gy = AGROUP ? ceil_div(na, FP0_WARPS) : (unsigned)na;
+      dim3 grid(gx, gy, ceil_div(g.H, 32 * R));
+      fp_z0_kernel<R, KW, AGROUP><<<grid, block, 0, stream>>>(x, y, angles, g, (int)a_base, y_lo,
+                                                              y_hi, accumulate);
       const cudaError_t e = cudaGetLastError();
       if (e != cudaSuccess) return e;
     }
   }
   return cudaSuccess;
+}
+
+template <int R>
+cudaError_t launch_fp_z0_variant(const float* x, float* y, const float* angles, const Geom& g,
+                                 cudaStream_t stream, int variant) {
+  switch (variant) {
+    case 1: return launch_fp_z0<R, 4, false>(x, y, angles, g, stream);
+    case 2: return launch_fp_z0<R, 8, false>(x, y, angles, g, stream);
+    case 3: return launch_fp_z0<R, 4, true>(x, y, angles, g, stream);
+    default: return launch_fp_z0<R, 8, true>(x, y, angles, g, stream);
+  }
+}
+
+// Variants: 1 = 4 bins per warp, warps of a block on neighbouring bins;
+// 2 = 8 bins, neighbouring bins; 3 = 4 bins, warps of a block on neighbouring
+// angles; 4 = 8 bins, neighbouring angles (default).
+cudaError_t launch_forward_z0(const float* x, float* y, const float* angles, const Geom& g,
+                              cudaStream_t stream) {
+  const bool vec4 = (g.Hx % 4 == 0) && (g.Hy % 4 == 0) &&
+                    ((reinterpret_cast<uintptr_t>(x) | reinterpret_cast<uintptr_t>(y)) & 15) == 0;
+  const int variant = kernel_variant(OP_FORWARD_Z0);
+  if (vec4) return launch_fp_z0_variant<4>(x, y, angles, g, stream, variant);
+  return launch_fp_z0_variant<1>(x, y, angles, g, stream, variant);
 }
 
 cudaError_t launch_forward_z2(const float* x, float* y, const float* angles, const Geom& g,

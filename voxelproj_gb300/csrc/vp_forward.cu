@@ -299,7 +299,7 @@ int fp0_slab_rows(const Geom& g) {
 int launches_forward_z0(const Geom& g) {
   const int rows = fp0_slab_rows(g);
   const int v = kernel_variant(OP_FORWARD_Z0);
-  const long long per = (v == 1 || v == 2) ? kMaxGridYZ : (long long)kMaxGridYZ * FP0_WARPS;
+  const long long per = (v == 3 || v == 4) ? (long long)kMaxGridYZ * FP0_WARPS : kMaxGridYZ;
   return (int)(ceil_div(g.SY, rows) * ceil_div(g.n_ang, per));
 }
 
@@ -338,16 +338,16 @@ template <int R>
 cudaError_t launch_fp_z0_variant(const float* x, float* y, const float* angles, const Geom& g,
                                  cudaStream_t stream, int variant) {
   switch (variant) {
-    case 1: return launch_fp_z0<R, 4, false>(x, y, angles, g, stream);
     case 2: return launch_fp_z0<R, 8, false>(x, y, angles, g, stream);
     case 3: return launch_fp_z0<R, 4, true>(x, y, angles, g, stream);
-    default: return launch_fp_z0<R, 8, true>(x, y, angles, g, stream);
+    case 4: return launch_fp_z0<R, 8, true>(x, y, angles, g, stream);
+    default: return launch_fp_z0<R, 4, false>(x, y, angles, g, stream);
   }
 }
 
-// Variants: 1 = 4 bins per warp, warps of a block on neighbouring bins;
-// 2 = 8 bins, neighbouring bins; 3 = 4 bins, warps of a block on neighbouring
-// angles; 4 = 8 bins, neighbouring angles (default).
+// Variants: 1 = 4 bins per warp, warps of a block on neighbouring bins
+// (default, fastest at 512^3); 2 = 8 bins, neighbouring bins; 3 = 4 bins,
+// warps of a block on neighbouring angles; 4 = 8 bins, neighbouring angles.
 cudaError_t launch_forward_z0(const float* x, float* y, const float* angles, const Geom& g,
                               cudaStream_t stream) {
   const bool vec4 = (g.Hx % 4 == 0) && (g.Hy % 4 == 0) &&

@@ -69,7 +69,7 @@ def adam_reconstruct(P: Projector, b: torch.Tensor, steps: int = 50, lr: float =
         loss = 0.5 * (r.double() ** 2).sum()
         loss.backward()
         opt.step()
-        losses.append(float(loss))
+        losses.append(float(loss.detach()))
     return x.detach(), losses
 
 

@@ -62,6 +62,7 @@ extern "C" {
 #define VP_ERR_BAD_Z_ORDER 6    /* z_order other than 0 or 2 */
 #define VP_ERR_WORKSPACE 7      /* workspace smaller than vp_z2_workspace_bytes() */
 #define VP_ERR_SCRATCH_LIMIT 8  /* problem too large for vp_forward_z2_noalloc's array */
+#define VP_ERR_BATCH 9          /* a batch problem this library cannot batch (see vp_batch_create) */
 
 /* Flags. */
 #define VP_FLAG_TRIG_PRECISE 1  /* accurate sincosf / IEEE division for the per-angle
@@ -148,6 +149,47 @@ VP_API int vp_backward_z2_ws(const float* y, int64_t y0, int64_t y1, int64_t y2,
 VP_API int vp_forward_z2_noalloc(const float* x, int64_t x0, int64_t x1, int64_t x2,
                                  float* y, int64_t y0, int64_t y1, int64_t y2,
                                  const float* angles, int64_t n_angles, int flags, void* stream);
+
+/* ---- Batches -----------------------------------------------------------
+ * Many problems of different sizes and angle counts, forward and adjoint
+ * mixed, in ONE persistent kernel launch.  No counterpart in the reference,
+ * which launches one kernel per call.
+ *
+ * A problem is in z_order 0 layout (x (SY, SX, H), y (n_ang, PX, H)) with
+ * heights a multiple of 4 and 16-byte aligned buffers; its output is
+ * accumulated into, as for the single-problem calls.  Outputs of different
+ * problems must not overlap.  The adjoint of a batch accumulates in the
+ * reference's order (bit-identical to backward variant 4); the forward has the
+ * single-problem kernel's weights. */
+#define VP_OP_FORWARD 0   /* out (y) += A in (x) */
+#define VP_OP_BACKWARD 1  /* out (x) += A^T in (y) */
+
+typedef struct vp_batch_problem {
+  int op;                 /* VP_OP_FORWARD or VP_OP_BACKWARD */
+  int flags;              /* VP_FLAG_* as for the single-problem calls */
+  int variant;            /* 0 = default; forward: 1 = 4 bins per warp, 2 = 8;
+                             adjoint: 4 = 2x2 voxel blocks, 3 = 4x2 */
+  int reserved;
+  const float* in;        /* x for a forward problem, y for an adjoint one */
+  float* out;             /* y for a forward problem, x for an adjoint one */
+  const float* angles;
+  int64_t n_angles;
+  int64_t in_dims[3];
+  int64_t out_dims[3];
+} vp_batch_problem;
+
+typedef struct vp_batch_plan vp_batch_plan;
+
+/* Validates the problems and uploads their descriptor table to the current
+ * device (the only device allocation); *plan receives the plan. */
+VP_API int vp_batch_create(const vp_batch_problem* problems, int count, vp_batch_plan** plan);
+/* Enqueues the whole batch on `stream`: a counter reset and one persistent
+ * launch.  Allocates and synchronises nothing, so it can be captured in a
+ * CUDA graph.  Runs of the same plan must not overlap on the GPU. */
+VP_API int vp_batch_run(vp_batch_plan* plan, void* stream);
+/* Work items of the plan (blocks' units of work). */
+VP_API int64_t vp_batch_work_items(const vp_batch_plan* plan);
+VP_API int vp_batch_destroy(vp_batch_plan* plan);
 
 /* z_order dispatch, as voxelproj.wrappers.forward/backward select a kernel by
  * z_order (voxelproj/wrappers.py:44-47, :92-95); dims as for the

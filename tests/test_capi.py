@@ -41,7 +41,7 @@ def test_binding_covers_header():
 
 
 def test_status_strings():
-    for code in range(0, 9):
+    for code in range(0, 10):
         assert _lib.LIB.vp_error_string(code)
     assert b"unknown" in _lib.LIB.vp_error_string(99)
 
@@ -76,3 +76,30 @@ def test_dispatch_rejects_bad_z_order():
         _lib.VP_ERR_BAD_Z_ORDER
     assert _lib.LIB.vp_backward(DUMMY, dims, DUMMY, dims, DUMMY, 10, 3, 0, None) == \
         _lib.VP_ERR_BAD_Z_ORDER
+
+
+def test_batch_validation_without_gpu():
+    lib = _lib.LIB
+    plan = ctypes.c_void_p()
+    p = _lib.BatchProblem()
+    p.op = 7  # unknown operation
+    arr = (_lib.BatchProblem * 1)(p)
+    assert lib.vp_batch_create(arr, 1, ctypes.byref(plan)) == _lib.VP_ERR_BATCH
+    p.op = _lib.VP_OP_FORWARD
+    p.in_, p.out, p.angles = 0x1000, 0x2000, 0x3000
+    p.n_angles = 10
+    p.in_dims[:] = [8, 8, 6]     # heights not a multiple of 4
+    p.out_dims[:] = [10, 8, 6]
+    arr = (_lib.BatchProblem * 1)(p)
+    assert lib.vp_batch_create(arr, 1, ctypes.byref(plan)) == _lib.VP_ERR_BATCH
+    p.in_dims[:] = [8, 8, 8]
+    p.out_dims[:] = [12, 8, 8]   # 12 angles, 10 given
+    arr = (_lib.BatchProblem * 1)(p)
+    assert lib.vp_batch_create(arr, 1, ctypes.byref(plan)) == _lib.VP_ERR_ANGLES
+    assert lib.vp_batch_run(None, None) == _lib.VP_ERR_NULL_POINTER
+    assert lib.vp_batch_destroy(None) == _lib.VP_OK
+
+
+def test_batch_problem_layout_matches_header():
+    # int op, flags, variant, reserved; 3 pointers; n_angles; 2 x int64[3]
+    assert ctypes.sizeof(_lib.BatchProblem) == 16 + 3 * 8 + 8 + 48

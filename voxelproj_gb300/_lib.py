@@ -21,6 +21,26 @@ VP_ERR_BAD_FLAGS = 5
 VP_ERR_BAD_Z_ORDER = 6
 VP_ERR_WORKSPACE = 7
 VP_ERR_SCRATCH_LIMIT = 8
+VP_ERR_BATCH = 9
+VP_OP_FORWARD = 0
+VP_OP_BACKWARD = 1
+
+
+class BatchProblem(ctypes.Structure):
+    """Mirror of vp_batch_problem (include/voxelproj_gb300.h)."""
+
+    _fields_ = [
+        ("op", ctypes.c_int),
+        ("flags", ctypes.c_int),
+        ("variant", ctypes.c_int),
+        ("reserved", ctypes.c_int),
+        ("in_", ctypes.c_void_p),
+        ("out", ctypes.c_void_p),
+        ("angles", ctypes.c_void_p),
+        ("n_angles", ctypes.c_int64),
+        ("in_dims", ctypes.c_int64 * 3),
+        ("out_dims", ctypes.c_int64 * 3),
+    ]
 VP_NOALLOC_SCRATCH_BYTES = 64 << 20
 
 VP_FLAG_TRIG_PRECISE = 1
@@ -48,6 +68,10 @@ SIGNATURES = {
                                ctypes.c_size_t, _P]),
     "vp_forward_z2_noalloc": (_I, [_P, _I64, _I64, _I64, _P, _I64, _I64, _I64, _P, _I64, _I,
                                    _P]),
+    "vp_batch_create": (_I, [_P, _I, _P]),
+    "vp_batch_run": (_I, [_P, _P]),
+    "vp_batch_work_items": (_I64, [_P]),
+    "vp_batch_destroy": (_I, [_P]),
     "vp_forward": (_I, [_P, _P, _P, _P, _P, _I64, _I, _I, _P]),
     "vp_backward": (_I, [_P, _P, _P, _P, _P, _I64, _I, _I, _P]),
 }

@@ -1,0 +1,174 @@
+"""Batched projections in one persistent launch, replayable as a CUDA graph.
+
+    b = Batch([("forward", x1, y1, angles1), ("backward", y2, x2, angles2, 4), ...])
+    b.run()                 # one persistent kernel launch for all problems
+    g = b.graph()           # CUDA graph of the same launch
+    g.replay()
+
+Each problem is (op, in, out, angles[, variant]): op "forward" adds A in to
+out, "backward" adds A^T in to out.  The tensors are CUDA float32 in z_order 0
+layout (x (SY, SX, H), y (n_ang, PX, H)) with H a multiple of 4; the batch
+keeps references to them.  Variants (None: chosen by the autotuner for cube
+problems, library default otherwise) select each problem's work-item body.
+
+    python -m voxelproj_gb300.batch
+
+runs the uneven-batch workload: 64 cubes with sides drawn from
+{64, 96, ..., 384} and U{90..720} angles each, A for every cube and A^T for
+every sinogram, in one persistent launch replayed as a CUDA graph, next to
+the same work issued as sequential single-problem calls.  It prints one JSON
+line.
+"""
+
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+
+import numpy as np
+import torch
+
+from . import _lib
+
+_OPS = {"forward": _lib.VP_OP_FORWARD, "backward": _lib.VP_OP_BACKWARD}
+
+
+def _problem(op, inp, out, angles, variant):
+    for t, name in ((inp, "in"), (out, "out"), (angles, "angles")):
+        if not (isinstance(t, torch.Tensor) and t.is_cuda and t.dtype == torch.float32
+                and t.is_contiguous()):
+            raise RuntimeError(f"batch {name} must be a contiguous float32 CUDA tensor")
+    if inp.dim() != 3 or out.dim() != 3:
+        raise RuntimeError("batch in/out must be 3-D (z_order 0 layout)")
+    p = _lib.BatchProblem()
+    p.op = _OPS[op]
+    p.flags = 0
+    p.variant = int(variant or 0)
+    p.in_ = inp.data_ptr()
+    p.out = out.data_ptr()
+    p.angles = angles.data_ptr()
+    p.n_angles = angles.numel()
+    p.in_dims[:] = list(inp.shape)
+    p.out_dims[:] = list(out.shape)
+    return p
+
+
+class Batch:
+    """A fixed batch of projection problems (see the module docstring)."""
+
+    def __init__(self, problems, device=None):
+        self._keep = []
+        probs = []
+        for spec in problems:
+            op, inp, out, angles = spec[:4]
+            variant = spec[4] if len(spec) > 4 else None
+            if op not in _OPS:
+                raise KeyError(op)
+            probs.append(_problem(op, inp, out, angles, variant))
+            self._keep.append((inp, out, angles))
+        self.device = torch.device(device) if device is not None else (
+            self._keep[0][0].device if self._keep else torch.device("cuda"))
+        arr = (_lib.BatchProblem * max(1, len(probs)))(*probs)
+        self._plan = ctypes.c_void_p()
+        with torch.cuda.device(self.device):
+            _lib.check(_lib.LIB.vp_batch_create(arr, len(probs), ctypes.byref(self._plan)),
+                       "batch_create")
+        self.work_items = int(_lib.LIB.vp_batch_work_items(self._plan))
+
+    def run(self, stream=None):
+        """Enqueue the whole batch (one persistent launch) on `stream`
+        (default: the current stream)."""
+        s = stream if stream is not None else torch.cuda.current_stream(self.device)
+        with torch.cuda.device(self.device):
+            _lib.check(_lib.LIB.vp_batch_run(self._plan, s.cuda_stream), "batch_run")
+
+    def graph(self) -> torch.cuda.CUDAGraph:
+        """Capture one run in a CUDA graph; replay() re-executes the batch."""
+        g = torch.cuda.CUDAGraph()
+        s = torch.cuda.Stream(self.device)
+        s.wait_stream(torch.cuda.current_stream(self.device))
+        with torch.cuda.stream(s):
+            with torch.cuda.graph(g, stream=s):
+                self.run(s)
+        torch.cuda.current_stream(self.device).wait_stream(s)
+        return g
+
+    def close(self):
+        if self._plan:
+            _lib.LIB.vp_batch_destroy(self._plan)
+            self._plan = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def uneven_cubes(count=64, seed=2026, sides=tuple(range(64, 385, 32)), nmin=90, nmax=720):
+    """(side, n_ang) of the uneven-batch workload, seeded."""
+    rng = np.random.default_rng(seed)
+    return [(int(rng.choice(sides)), int(rng.integers(nmin, nmax + 1))) for _ in range(count)]
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawTextHelpFormatter)
+    ap.add_argument("--count", type=int, default=64)
+    ap.add_argument("--reps", type=int, default=5)
+    ap.add_argument("--no-tune", action="store_true")
+    args = ap.parse_args()
+    from . import _CU, tune
+
+    dev = torch.device("cuda")
+    shapes = uneven_cubes(args.count)
+    g = torch.Generator(device=dev).manual_seed(7)
+    problems, plain = [], []
+    vu = 0
+    for side, n in shapes:
+        ang = torch.linspace(0, np.pi, n + 1, device=dev)[:-1].contiguous()
+        x = torch.randn(side, side, side, device=dev, generator=g)
+        y = torch.randn(n, side, side, device=dev, generator=g)
+        y_out = torch.zeros(n, side, side, device=dev)
+        x_out = torch.zeros(side, side, side, device=dev)
+        vf = None if args.no_tune else tune.batch_variant("forward", side, n)
+        vb = None if args.no_tune else tune.batch_variant("backward", side, n)
+        problems += [("forward", x, y_out, ang, vf), ("backward", y, x_out, ang, vb)]
+        plain.append((x, y_out, y, x_out, ang))
+        vu += 2 * side**3 * n
+    batch = Batch(problems)
+    graph = batch.graph()
+
+    def timed(fn):
+        fn()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        for _ in range(args.reps):
+            fn()
+        b.record()
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / args.reps
+
+    t_graph = timed(graph.replay)
+
+    def sequential():
+        for x, y_out, y, x_out, ang in plain:
+            _CU.forward_z0(x, y_out, ang)
+            _CU.backward_z0(y, x_out, ang)
+
+    t_seq = timed(sequential)
+    print(json.dumps({
+        "workload": f"{args.count} cubes, sides {{64..384 step 32}}, U{{90..720}} angles each; "
+                    "A of every cube and A^T of every sinogram",
+        "voxel_angle_updates": vu, "work_items": batch.work_items,
+        "graph_ms": round(t_graph, 3), "graph_gvu_s": round(vu / t_graph / 1e6, 1),
+        "sequential_ms": round(t_seq, 3), "sequential_gvu_s": round(vu / t_seq / 1e6, 1),
+        "speedup_vs_sequential": round(t_seq / t_graph, 3),
+        "launches_per_batch": 1,
+    }))
+    batch.close()
+
+
+if __name__ == "__main__":
+    main()

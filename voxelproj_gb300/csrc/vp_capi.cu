@@ -99,6 +99,13 @@ int finish(cudaError_t e, int launches) {
 }  // namespace
 
 namespace vp {
+int record_cuda_error(cudaError_t e) {
+  g_last_cuda_error = (int)e;
+  return VP_ERR_CUDA;
+}
+
+void count_launches(int n) { g_launches.fetch_add((uint64_t)n, std::memory_order_relaxed); }
+
 int kernel_variant(int op) {
   return (op >= 0 && op < OP_COUNT) ? g_variant[op].load(std::memory_order_relaxed) : 0;
 }
@@ -127,6 +134,9 @@ const char* vp_error_string(int status) {
     case VP_ERR_BAD_FLAGS: return "unknown flag bits";
     case VP_ERR_BAD_Z_ORDER: return "z_order must be 0 or 2";
     case VP_ERR_WORKSPACE: return "workspace smaller than vp_z2_workspace_bytes()";
+    case VP_ERR_BATCH:
+      return "unsupported batch problem (z_order 0 with heights in multiples of 4 and "
+             "16-byte aligned buffers, op VP_OP_FORWARD or VP_OP_BACKWARD)";
     case VP_ERR_SCRATCH_LIMIT:
       return "problem needs more scratch than the library's static array holds "
              "(VP_NOALLOC_SCRATCH_BYTES); use vp_forward_z2 or vp_forward_z2_ws";

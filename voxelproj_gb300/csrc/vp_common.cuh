@@ -178,6 +178,23 @@ __device__ __forceinline__ float vzero<float>() { return 0.0f; }
 template <>
 __device__ __forceinline__ float4 vzero<float4>() { return make_float4(0.f, 0.f, 0.f, 0.f); }
 
+// Float vector of R heights per lane (R = 1 or 4) and a guarded load of it.
+template <int R>
+struct Vec;
+template <>
+struct Vec<1> {
+  using T = float;
+};
+template <>
+struct Vec<4> {
+  using T = float4;
+};
+
+template <typename V>
+__device__ __forceinline__ V ld_or_zero(const float* p, bool ok) {
+  return ok ? __ldg(reinterpret_cast<const V*>(p)) : vzero<V>();
+}
+
 // Geometry shared by all launches.  Volume (SY, SX) comes from x, detector
 // (n_ang, PX) from y; H is min(Hx, Hy): heights past the shorter array read
 // as zero in the reference (border-mode texture) and so leave the output

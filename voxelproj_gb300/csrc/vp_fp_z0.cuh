@@ -1,0 +1,186 @@
+// Per-warp body of the z_order 0 forward projection (detector-driven
+// gather), shared by the single-problem kernel (vp_forward.cu) and the
+// batched persistent kernel (vp_batch.cu).  See vp_forward.cu for the design.
+#pragma once
+
+#include "vp_common.cuh"
+
+namespace vp {
+namespace detail {
+
+constexpr float kWindowMargin = 1e-3f;
+
+// Minor-axis index range [lo, hi] (clamped to [0, n_minor)) of voxels on major
+// line i whose detector coordinate can fall in [t_lo, t_hi].
+struct MinorRange {
+  int lo, hi;
+};
+
+__device__ __forceinline__ MinorRange minor_range(int i, float cent_major, float sh_major,
+                                                  float cent_minor, float inv_sh_minor,
+                                                  int min_lo, int min_hi, float pcent,
+                                                  float t_lo, float t_hi) {
+  const float K = ((float)i - cent_major) * sh_major + pcent;
+  const float u1 = (t_lo - K) * inv_sh_minor + cent_minor;
+  const float u2 = (t_hi - K) * inv_sh_minor + cent_minor;
+  MinorRange m;
+  m.lo = max(min_lo, (int)ceilf(fminf(u1, u2)));
+  m.hi = min(min_hi, (int)floorf(fmaxf(u1, u2)));
+  return m;
+}
+
+// ---------------------------------------------------------------------------
+// z_order 0: x (SY, SX, H), y (n_ang, PX, H); heights contiguous.
+// A warp owns angle a, KW consecutive bins and 32*R heights (lane <->
+// heights).  The voxels gathered are warp-uniform, so the warp enumerates
+// them cooperatively: lane j takes major line i0+j, computes its candidate
+// voxels and their bin weights into a per-warp shared list (offsets from a
+// warp prefix sum), then all lanes stream the list with broadcast reads,
+// FP0_UNROLL candidates at a time so their loads overlap, and accumulate
+// the KW bins in registers.  A candidate's three bins sit at run-relative
+// offsets q-2, q-1, q (q = round(xp) - p0 + 1), dispatched with a
+// warp-uniform switch.
+//
+// Cache locality: every angle touches the whole volume, so a launch is
+// restricted to one slab of rows [y_lo, y_hi) of the volume (all launches add
+// into y), and heights are the slowest grid axis.  Concurrently running
+// blocks then share one slab x one 128-height chunk, a few tens of MB that
+// stay in L2 across all angles instead of being re-read from HBM per angle.
+// With AGROUP the four warps of a block take four consecutive angles of the
+// same bins: their voxel strips largely coincide, so one warp's loads are L1
+// hits for the others.
+// ---------------------------------------------------------------------------
+constexpr int FP0_WARPS = 4;
+constexpr int FP0_QBITS = 4;   // q in [0, KW + 1]
+constexpr int FP0_UNROLL = 4;  // candidates whose loads are in flight together
+
+// >= max candidates per major line: floor((KW + 2b + margin) / sqrt(1/2)) + 1
+template <int KW>
+struct Fp0Cap {
+  static constexpr int value = KW == 4 ? 10 : 15;
+  static_assert(KW == 4 || KW == 8, "bins per warp: 4 or 8");
+  static_assert(KW + 1 < (1 << FP0_QBITS), "q must fit its bits");
+};
+
+// Adds a candidate's weights to the run's accumulators: bin q-2 gets w0, q-1
+// gets w1, q gets w2 (run-relative); bins outside [0, KW) are dropped.
+template <int KW, int Q, typename V>
+__device__ __forceinline__ void scatter3(V (&acc)[KW], const float4& e, const V& xv) {
+  if constexpr (Q - 2 >= 0 && Q - 2 < KW) acc[Q - 2] = f4_fma(e.x, xv, acc[Q - 2]);
+  if constexpr (Q - 1 >= 0 && Q - 1 < KW) acc[Q - 1] = f4_fma(e.y, xv, acc[Q - 1]);
+  if constexpr (Q < KW) acc[Q] = f4_fma(e.z, xv, acc[Q]);
+}
+
+template <int KW, typename V>
+__device__ __forceinline__ void scatter_q(V (&acc)[KW], const float4& e, const V& xv, int q) {
+#define VP_Q_CASE(Q)                                            \
+  case Q:                                                       \
+    if constexpr (Q <= KW + 1) scatter3<KW, Q>(acc, e, xv);     \
+    break;
+  switch (q) {
+    VP_Q_CASE(0) VP_Q_CASE(1) VP_Q_CASE(2) VP_Q_CASE(3) VP_Q_CASE(4)
+    VP_Q_CASE(5) VP_Q_CASE(6) VP_Q_CASE(7) VP_Q_CASE(8) VP_Q_CASE(9)
+    default: break;
+  }
+#undef VP_Q_CASE
+}
+
+// One warp: angle a, bins [p0, p0 + KW), heights [h, h + R) of this lane,
+// volume rows [y_lo, y_hi).  cand is this warp's shared candidate list of
+// 32 * Fp0Cap<KW>::value entries.  All 32 lanes must call it together.
+template <int R, int KW>
+__device__ __forceinline__ void fp_z0_warp(const float* __restrict__ x, float* __restrict__ y,
+                                           const float* __restrict__ angles, const Geom& g,
+                                           int p0, int a, int h, int y_lo, int y_hi,
+                                           int accumulate, float4* cand) {
+  using V = typename Vec<R>::T;
+  constexpr int CAP = Fp0Cap<KW>::value;
+  const int lane = threadIdx.x & 31;
+  if (p0 >= g.PX || a >= g.n_ang) return;  // warp-uniform
+  const bool hv = h < g.H;
+
+  const AngleConst k = angle_const(__ldg(angles + a), g.trig);
+  const bool minor_x = fabsf(k.c) >= fabsf(k.s);
+  // major lines [maj_lo, maj_hi), minor indices [min_lo, min_hi], within the slab
+  const int maj_lo = minor_x ? y_lo : 0;
+  const int maj_hi = minor_x ? y_hi : g.SX;
+  const int min_lo = minor_x ? 0 : y_lo;
+  const int min_hi = minor_x ? g.SX - 1 : y_hi - 1;
+  const float cent_major = minor_x ? g.ycent : g.xcent;
+  const float cent_minor = minor_x ? g.xcent : g.ycent;
+  const float sh_major = minor_x ? k.s : k.c;
+  const float inv_sh_minor = 1.0f / (minor_x ? k.c : k.s);
+  const float t_lo = (float)p0 - 0.5f - k.b - kWindowMargin;
+  const float t_hi = (float)(p0 + KW) - 0.5f + k.b + kWindowMargin;
+
+  V acc[KW];
+#pragma unroll
+  for (int b = 0; b < KW; ++b) acc[b] = vzero<V>();
+  const int hs = hv ? h : 0;  // idle lanes read row 0 (always valid) and never store
+
+  for (int i0 = maj_lo; i0 < maj_hi; i0 += 32) {
+    const int i = i0 + lane;
+    int lo = 0, cnt = 0;
+    if (i < maj_hi) {
+      const MinorRange mr = minor_range(i, cent_major, sh_major, cent_minor, inv_sh_minor,
+                                        min_lo, min_hi, g.pcent, t_lo, t_hi);
+      lo = mr.lo;
+      cnt = max(0, min(mr.hi - mr.lo + 1, CAP));
+    }
+    int incl = cnt;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const int n = __shfl_up_sync(0xffffffffu, incl, d);
+      if (lane >= d) incl += n;
+    }
+    const int total = __shfl_sync(0xffffffffu, incl, 31);
+    const int start = incl - cnt;
+    for (int t = 0; t < cnt; ++t) {
+      const int m = lo + t;
+      const int xi = minor_x ? m : i;
+      const int yi = minor_x ? i : m;
+      const BinWeights bw =
+          voxel_weights((float)xi - g.xcent, (float)yi - g.ycent, k, g.pcent, g.trig);
+      int q = bw.r - p0 + 1;
+      float4 e = make_float4(bw.w0, bw.w1, bw.w2, 0.0f);
+      if (q < 0 || q > KW + 1) {
+        q = 0;
+        e = make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+      const int vox = yi * g.SX + xi;
+      e.w = __int_as_float((vox << FP0_QBITS) | q);
+      cand[start + t] = e;
+    }
+    __syncwarp();
+    for (int c0 = 0; c0 < total; c0 += FP0_UNROLL) {
+      float4 e[FP0_UNROLL];
+      V xv[FP0_UNROLL];
+#pragma unroll
+      for (int u = 0; u < FP0_UNROLL; ++u) {
+        e[u] = (c0 + u < total) ? cand[c0 + u] : make_float4(0.f, 0.f, 0.f, 0.f);
+        const int vox = __float_as_int(e[u].w) >> FP0_QBITS;
+        xv[u] = __ldg(reinterpret_cast<const V*>(x + (size_t)vox * g.Hx + hs));
+      }
+#pragma unroll
+      for (int u = 0; u < FP0_UNROLL; ++u) {
+        if (c0 + u >= total) break;  // padding slots (warp-uniform)
+        scatter_q<KW>(acc, e[u], xv[u], __float_as_int(e[u].w) & ((1 << FP0_QBITS) - 1));
+      }
+    }
+    __syncwarp();
+  }
+
+  if (hv) {
+#pragma unroll
+    for (int b = 0; b < KW; ++b) {
+      const int p = p0 + b;
+      if (p < g.PX) {
+        V* py = reinterpret_cast<V*>(y + ((size_t)a * g.PX + p) * g.Hy + h);
+        store_out(py, acc[b], accumulate);
+      }
+    }
+  }
+}
+
+}  // namespace detail
+}  // namespace vp

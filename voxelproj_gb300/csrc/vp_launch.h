@@ -20,6 +20,12 @@ cudaError_t launch_backward_z0(const float* y, float* x, const float* angles, co
 cudaError_t launch_backward_z2(const float* y, float* x, const float* angles, const Geom& g,
                                cudaStream_t stream);
 
+// Status bookkeeping shared by the C entry points (vp_capi.cu): records a
+// CUDA error for vp_last_cuda_error() and returns VP_ERR_CUDA; counts launches
+// for vp_launch_count().
+int record_cuda_error(cudaError_t e);
+void count_launches(int n);
+
 // Kernel variant selection (0 = automatic), set through vp_set_kernel_variant.
 enum Op : int { OP_FORWARD_Z0 = 0, OP_BACKWARD_Z0 = 1, OP_FORWARD_Z2 = 2, OP_BACKWARD_Z2 = 3,
                 OP_COUNT = 4 };

@@ -158,17 +158,18 @@ VP_API int vp_forward_z2_noalloc(const float* x, int64_t x0, int64_t x1, int64_t
  * A problem is in z_order 0 layout (x (SY, SX, H), y (n_ang, PX, H)) with
  * heights a multiple of 4 and 16-byte aligned buffers; its output is
  * accumulated into, as for the single-problem calls.  Outputs of different
- * problems must not overlap.  The adjoint of a batch accumulates in the
- * reference's order (bit-identical to backward variant 4); the forward has the
- * single-problem kernel's weights. */
+ * problems must not overlap.  Results equal the single-problem kernels of the
+ * same variant, bit for bit. */
 #define VP_OP_FORWARD 0   /* out (y) += A in (x) */
 #define VP_OP_BACKWARD 1  /* out (x) += A^T in (y) */
 
 typedef struct vp_batch_problem {
   int op;                 /* VP_OP_FORWARD or VP_OP_BACKWARD */
   int flags;              /* VP_FLAG_* as for the single-problem calls */
-  int variant;            /* 0 = default; forward: 1 = 4 bins per warp, 2 = 8;
-                             adjoint: 4 = 2x2 voxel blocks, 3 = 4x2 */
+  int variant;            /* 0 = default; forward: 1 (4 bins per warp, volume
+                             slabs); adjoint: 6 = runs in two angle classes
+                             (default), 4 = 2x2 voxel blocks (accumulates in the
+                             reference's order, bit-identical to it) */
   int reserved;
   const float* in;        /* x for a forward problem, y for an adjoint one */
   float* out;             /* y for a forward problem, x for an adjoint one */
@@ -189,6 +190,10 @@ VP_API int vp_batch_create(const vp_batch_problem* problems, int count, vp_batch
 VP_API int vp_batch_run(vp_batch_plan* plan, void* stream);
 /* Work items of the plan (blocks' units of work). */
 VP_API int64_t vp_batch_work_items(const vp_batch_plan* plan);
+/* Synchronises and reports whether a run hit its bounded wait between stages
+ * (*error = 1: a dependency did not complete in ~4 s and the result may be
+ * wrong).  Stays set for the plan's lifetime once raised. */
+VP_API int vp_batch_error(vp_batch_plan* plan, int* error);
 VP_API int vp_batch_destroy(vp_batch_plan* plan);
 
 /* z_order dispatch, as voxelproj.wrappers.forward/backward select a kernel by

@@ -30,8 +30,10 @@ def _inputs(geoms, seed):
     return out
 
 
-@pytest.mark.parametrize("vf,vb", [(1, 4), (2, 3)])
+@pytest.mark.parametrize("vf,vb", [(1, 4), (1, 6), (0, 0)])
 def test_batch_matches_single_problem_calls(vf, vb):
+    """Same bodies, same slabs and stages, same order: the batch reproduces the
+    single-problem kernels of the same variant bit for bit."""
     cases = _inputs(GEOMS, 100)
     problems, outs = [], []
     for c in cases:
@@ -45,20 +47,52 @@ def test_batch_matches_single_problem_calls(vf, vb):
     b = Batch(problems)
     b.run()
     torch.cuda.synchronize()
-    _lib.LIB.vp_set_kernel_variant(1, 4)  # single-problem adjoint in the reference's order
+    assert not b.error()
+    _lib.LIB.vp_set_kernel_variant(1, vb)
     try:
         for c, (yo, xo) in zip(cases, outs):
             SY, SX, H, n, PX = c["geom"]
             a = torch.tensor(c["ang"], device="cuda")
             xs = torch.zeros_like(xo)
             vp._CU.backward_z0(torch.tensor(c["y"], device="cuda"), xs, a)
+            ys = torch.tensor(c["y0"], device="cuda")
+            vp._CU.forward_z0(torch.tensor(c["x"], device="cuda"), ys, a)
             torch.cuda.synchronize()
-            # same order of accumulation as the 2x2 / 4x2 block bodies: identical
             assert torch.equal(xo, xs)
+            assert torch.equal(yo, ys)
             Ax = oracle.forward(c["x"], c["ang"], PX, 0)
             assert rel_err(yo.cpu().numpy() - c["y0"], Ax) <= tol.ref_vs_fp64(max(SY, SX, PX))
     finally:
         _lib.LIB.vp_set_kernel_variant(1, 0)
+    b.close()
+
+
+def test_batch_stages_on_large_problems():
+    """Problems with several volume slabs (forward stages) and both angle
+    classes (adjoint stages) in one launch, against single-problem calls."""
+    probs, refs = [], []
+    for side, n in [(320, 60), (200, 45), (96, 30)]:
+        a = torch.linspace(0, np.pi, n + 1, device="cuda")[:-1].contiguous()
+        x = torch.randn(side, side, 132, device="cuda")
+        y = torch.randn(n, side, 132, device="cuda")
+        yo = torch.zeros(n, side, 132, device="cuda")
+        xo = torch.zeros(side, side, 132, device="cuda")
+        probs += [("forward", x, yo, a), ("backward", y, xo, a)]
+        refs.append((x, y, yo, xo, a))
+    b = Batch(probs)
+    b.run()
+    b.run()  # runs accumulate: every output is now twice the operator
+    torch.cuda.synchronize()
+    assert not b.error()
+    for x, y, yo, xo, a in refs:
+        ys = torch.zeros_like(yo)
+        xs = torch.zeros_like(xo)
+        for _ in range(2):
+            vp._CU.forward_z0(x, ys, a)
+            vp._CU.backward_z0(y, xs, a)
+        torch.cuda.synchronize()
+        assert torch.equal(yo, ys)
+        assert torch.equal(xo, xs)
     b.close()
 
 

@@ -71,6 +71,7 @@ SIGNATURES = {
     "vp_batch_create": (_I, [_P, _I, _P]),
     "vp_batch_run": (_I, [_P, _P]),
     "vp_batch_work_items": (_I64, [_P]),
+    "vp_batch_error": (_I, [_P, _P]),
     "vp_batch_destroy": (_I, [_P]),
     "vp_forward": (_I, [_P, _P, _P, _P, _P, _I64, _I, _I, _P]),
     "vp_backward": (_I, [_P, _P, _P, _P, _P, _I64, _I, _I, _P]),

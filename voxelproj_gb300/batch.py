@@ -94,6 +94,14 @@ class Batch:
         torch.cuda.current_stream(self.device).wait_stream(s)
         return g
 
+    def error(self) -> bool:
+        """Synchronises; True if a run hit the bounded wait between stages
+        (a dependency did not complete in time; results may be wrong)."""
+        flag = ctypes.c_int(0)
+        with torch.cuda.device(self.device):
+            _lib.check(_lib.LIB.vp_batch_error(self._plan, ctypes.byref(flag)), "batch_error")
+        return bool(flag.value)
+
     def close(self):
         if self._plan:
             _lib.LIB.vp_batch_destroy(self._plan)

@@ -15,6 +15,7 @@
 #include <cuda_runtime.h>
 
 #include "vp_bp_block.cuh"
+#include "vp_bp_runs.cuh"
 #include "vp_common.cuh"
 #include "vp_launch.h"
 
@@ -153,55 +154,6 @@ __global__ void __launch_bounds__(32 * BPB_WARPS)
 // saw no angle of its class leaves x untouched (in store mode the first launch
 // always writes).
 // ---------------------------------------------------------------------------
-constexpr int RUN = 4;
-constexpr int BPR_WARPS = 4;
-constexpr int BPR_CHUNK = 32;
-constexpr int BPR_LIST = 1024;  // class angles listed per window of the angle axis
-constexpr int BPR_GENERIC = 8;  // pattern value of the generic path
-
-struct RunEntry {
-  float4 w[3];  // weights of voxels 0..3, 3 each, in window order
-  int4 r;       // bin round(xp) of each voxel
-  int4 meta;    // element offset of the window's first bin (lo, hi), signed
-                // element step between window bins, pattern
-};
-
-// Fast path for advance pattern PAT: loads the W = 3 + popcount(PAT) window
-// bins with no predicates (the table phase routed windows that leave the
-// detector to the generic path), then applies the four voxels' weights.
-// p points at the window's first bin for this lane's heights; stride is the
-// signed distance between consecutive window bins.
-template <int PAT>
-__device__ __forceinline__ void run_window(float4 (&acc)[RUN], const float4 (&wv)[3],
-                                           const float* p, ptrdiff_t stride) {
-  constexpr int o1 = (PAT & 1);
-  constexpr int o2 = o1 + ((PAT >> 1) & 1);
-  constexpr int o3 = o2 + ((PAT >> 2) & 1);
-  constexpr int W = 3 + o3;
-  float4 win[W];
-#pragma unroll
-  for (int u = 0; u < W; ++u) win[u] = __ldg(reinterpret_cast<const float4*>(p + u * stride));
-  const float ws[12] = {wv[0].x, wv[0].y, wv[0].z, wv[0].w, wv[1].x, wv[1].y,
-                        wv[1].z, wv[1].w, wv[2].x, wv[2].y, wv[2].z, wv[2].w};
-  constexpr int off[RUN] = {0, o1, o2, o3};
-#pragma unroll
-  for (int m = 0; m < RUN; ++m) {
-#pragma unroll
-    for (int k = 0; k < 3; ++k) acc[m] = f4_fma(ws[3 * m + k], win[off[m] + k], acc[m]);
-  }
-}
-
-template <int PASS>
-__device__ __forceinline__ bool in_class(float phi, int trig) {
-  float s, c;
-  if (trig == TRIG_REF) {
-    __sincosf(phi, &s, &c);
-  } else {
-    sincosf(phi, &s, &c);
-  }
-  return (PASS == 0) == (fabsf(c) <= fabsf(s));
-}
-
 template <int PASS>
 __global__ void __launch_bounds__(32 * BPR_WARPS)
     bp_z0_runs_kernel(const float* __restrict__ y, float* __restrict__ x,
@@ -209,140 +161,15 @@ __global__ void __launch_bounds__(32 * BPR_WARPS)
                       int accumulate) {
   __shared__ RunEntry tab[BPR_WARPS][BPR_CHUNK];
   __shared__ int alist[BPR_WARPS][BPR_LIST];
-
   const int lane = threadIdx.x;
   const int w = threadIdx.y;
   const int run = blockIdx.x * BPR_WARPS + w;
   if (run >= nruns) return;  // warp-uniform; all shared state is per warp
-  const int h = (blockIdx.y * 32 + lane) * 4;
-  const bool hv = h < g.H;
-  const int hs = hv ? h : 0;  // idle lanes read valid memory and never store
   // PASS 0: run along x starting at (xi0, yi0); PASS 1: along y.
   const int xi0 = PASS == 0 ? (run % nrun_major) * RUN : run % nrun_major;
   const int yi0 = PASS == 0 ? run / nrun_major : (run / nrun_major) * RUN;
-  const int dx = PASS == 0 ? 1 : 0;
-  const int dy = PASS == 0 ? 0 : 1;
-
-  float4 acc[RUN];
-#pragma unroll
-  for (int m = 0; m < RUN; ++m) acc[m] = vzero<float4>();
-
-  const long long yrow = (long long)g.PX * g.Hy;
-  int seen = 0;
-
-  for (int w0 = 0; w0 < g.n_ang; w0 += BPR_LIST) {
-    // this warp's list of the class's angles in [w0, w0 + BPR_LIST), ascending
-    const int wend = min(g.n_ang, w0 + BPR_LIST);
-    int nlist = 0;
-    for (int a1 = w0; a1 < wend; a1 += 32) {
-      const int a = a1 + lane;
-      const bool mine = a < wend && in_class<PASS>(angles[a], g.trig);
-      const unsigned mask = __ballot_sync(0xffffffffu, mine);
-      if (mine) alist[w][nlist + __popc(mask & ((1u << lane) - 1u))] = a;
-      nlist += __popc(mask);
-    }
-    __syncwarp();
-
-    for (int c0 = 0; c0 < nlist; c0 += BPR_CHUNK) {
-      const int count = min(BPR_CHUNK, nlist - c0);
-      if (lane < count) {
-        const int a = alist[w][c0 + lane];
-        const AngleConst k = angle_const(angles[a], g.trig);
-        BinWeights bw[RUN];
-#pragma unroll
-        for (int m = 0; m < RUN; ++m) {
-          const float relx = (float)(xi0 + m * dx) - g.xcent;
-          const float rely = (float)(yi0 + m * dy) - g.ycent;
-          bw[m] = voxel_weights(relx, rely, k, g.pcent, g.trig);
-        }
-        const float step = PASS == 0 ? k.c : k.s;
-        const int dir = step >= 0.0f ? 1 : -1;
-        int pattern = 0;
-        bool ok = true;
-#pragma unroll
-        for (int m = 0; m + 1 < RUN; ++m) {
-          const int d = dir * (bw[m + 1].r - bw[m].r);
-          ok = ok && (d == 0 || d == 1);
-          pattern |= (d == 1 ? 1 : 0) << m;
-        }
-        // the fast path needs every window bin on the detector
-        const int base = bw[0].r - dir;
-        const int last = base + dir * (2 + __popc(pattern));
-        ok = ok && (unsigned)base < (unsigned)g.PX && (unsigned)last < (unsigned)g.PX;
-        float ws[12];
-#pragma unroll
-        for (int m = 0; m < RUN; ++m) {
-          // window order: increasing u, bin = base + dir * u
-          ws[3 * m + 0] = dir > 0 ? bw[m].w0 : bw[m].w2;
-          ws[3 * m + 1] = bw[m].w1;
-          ws[3 * m + 2] = dir > 0 ? bw[m].w2 : bw[m].w0;
-        }
-        RunEntry e;
-        e.w[0] = make_float4(ws[0], ws[1], ws[2], ws[3]);
-        e.w[1] = make_float4(ws[4], ws[5], ws[6], ws[7]);
-        e.w[2] = make_float4(ws[8], ws[9], ws[10], ws[11]);
-        e.r = make_int4(bw[0].r, bw[1].r, bw[2].r, bw[3].r);
-        const long long off = (long long)a * yrow + (long long)base * g.Hy;
-        e.meta = make_int4((int)(unsigned)(off & 0xffffffffll), (int)(off >> 32), dir * g.Hy,
-                           ok ? pattern : BPR_GENERIC);
-        tab[w][lane] = e;
-      }
-      __syncwarp();
-      for (int j = 0; j < count; ++j) {
-        const RunEntry& e = tab[w][j];
-        const int4 meta = e.meta;
-        const float4 wv[3] = {e.w[0], e.w[1], e.w[2]};
-        const long long off =
-            (long long)(unsigned)meta.x | ((long long)meta.y << 32);
-        const float* p = y + off + hs;
-        const ptrdiff_t stride = meta.z;
-        switch (meta.w) {
-          case 0: run_window<0>(acc, wv, p, stride); break;
-          case 1: run_window<1>(acc, wv, p, stride); break;
-          case 2: run_window<2>(acc, wv, p, stride); break;
-          case 3: run_window<3>(acc, wv, p, stride); break;
-          case 4: run_window<4>(acc, wv, p, stride); break;
-          case 5: run_window<5>(acc, wv, p, stride); break;
-          case 6: run_window<6>(acc, wv, p, stride); break;
-          case 7: run_window<7>(acc, wv, p, stride); break;
-          default: {
-            // generic path: three guarded loads per voxel, bins relative to
-            // the window start (p), whose bin is r0 - dir
-            const int dir = meta.z >= 0 ? 1 : -1;
-            const int rr[RUN] = {e.r.x, e.r.y, e.r.z, e.r.w};
-            const int base = rr[0] - dir;
-            const float ws[12] = {wv[0].x, wv[0].y, wv[0].z, wv[0].w, wv[1].x, wv[1].y,
-                                  wv[1].z, wv[1].w, wv[2].x, wv[2].y, wv[2].z, wv[2].w};
-#pragma unroll
-            for (int m = 0; m < RUN; ++m) {
-#pragma unroll
-              for (int kk = 0; kk < 3; ++kk) {
-                const int bin = rr[m] + dir * (kk - 1);
-                const float4 v = ld_or_zero<float4>(p + (ptrdiff_t)(bin - base) * g.Hy,
-                                                    (unsigned)bin < (unsigned)g.PX);
-                acc[m] = f4_fma(ws[3 * m + kk], v, acc[m]);
-              }
-            }
-            break;
-          }
-        }
-      }
-      __syncwarp();
-    }
-    seen += nlist;
-  }
-
-  if (hv && (seen > 0 || !accumulate)) {
-#pragma unroll
-    for (int m = 0; m < RUN; ++m) {
-      const int xi = xi0 + m * dx;
-      const int yi = yi0 + m * dy;
-      if (xi < g.SX && yi < g.SY) {
-        float4* px = reinterpret_cast<float4*>(x + ((size_t)yi * g.SX + xi) * g.Hx + h);
-        store_out(px, acc[m], accumulate);
-      }
-    }
-  }
+  bp_runs_warp<PASS>(y, x, angles, g, xi0, yi0, (blockIdx.y * 32 + lane) * 4, accumulate,
+                     tab[w], alist[w]);
 }
 
 // ---------------------------------------------------------------------------

@@ -217,4 +217,17 @@ __device__ __forceinline__ void store_out(float* p, float v, int accumulate) {
   *p = accumulate ? *p + v : v;
 }
 
+// Epilogue whose read bypasses L1 (ld.global.cg): for outputs that another
+// block of the same launch wrote before signalling completion, since L1 is
+// not coherent across SMs.
+__device__ __forceinline__ void store_out_coherent(float4* p, float4 v) {
+  *p = f4_add(__ldcg(p), v);
+}
+
+// Pre-store hook that does nothing (single-problem kernels).
+struct NoWait {
+  __device__ __forceinline__ void operator()() const {}
+  static constexpr bool coherent = false;
+};
+
 }  // namespace vp

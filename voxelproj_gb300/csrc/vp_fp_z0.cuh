@@ -88,15 +88,21 @@ __device__ __forceinline__ void scatter_q(V (&acc)[KW], const float4& e, const V
 // One warp: angle a, bins [p0, p0 + KW), heights [h, h + R) of this lane,
 // volume rows [y_lo, y_hi).  cand is this warp's shared candidate list of
 // 32 * Fp0Cap<KW>::value entries.  All 32 lanes must call it together.
-template <int R, int KW>
+// wait() runs (by the whole warp) just before the outputs are written; with
+// Wait::coherent the read of the output bypasses L1.
+template <int R, int KW, class Wait = NoWait>
 __device__ __forceinline__ void fp_z0_warp(const float* __restrict__ x, float* __restrict__ y,
                                            const float* __restrict__ angles, const Geom& g,
                                            int p0, int a, int h, int y_lo, int y_hi,
-                                           int accumulate, float4* cand) {
+                                           int accumulate, float4* cand,
+                                           const Wait& wait = Wait()) {
   using V = typename Vec<R>::T;
   constexpr int CAP = Fp0Cap<KW>::value;
   const int lane = threadIdx.x & 31;
-  if (p0 >= g.PX || a >= g.n_ang) return;  // warp-uniform
+  if (p0 >= g.PX || a >= g.n_ang) {  // warp-uniform
+    wait();
+    return;
+  }
   const bool hv = h < g.H;
 
   const AngleConst k = angle_const(__ldg(angles + a), g.trig);
@@ -170,13 +176,17 @@ __device__ __forceinline__ void fp_z0_warp(const float* __restrict__ x, float* _
     __syncwarp();
   }
 
+  wait();
   if (hv) {
 #pragma unroll
     for (int b = 0; b < KW; ++b) {
       const int p = p0 + b;
       if (p < g.PX) {
         V* py = reinterpret_cast<V*>(y + ((size_t)a * g.PX + p) * g.Hy + h);
-        store_out(py, acc[b], accumulate);
+        if constexpr (Wait::coherent && R == 4)
+          store_out_coherent(py, acc[b]);
+        else
+          store_out(py, acc[b], accumulate);
       }
     }
   }

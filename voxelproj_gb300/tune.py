@@ -7,8 +7,8 @@ the angle count, so shapes are tuned with at most 90 angles.
 
 Two consumers:
 * ``batch_variant(op, side, n_ang)`` chooses the work-item body of a batched
-  problem (forward: 4 or 8 bins per warp; adjoint: 2x2 or 4x2 voxel blocks),
-  timed as a one-problem batch;
+  problem (adjoint: runs in two angle classes or 2x2 voxel blocks; the
+  forward has one body), timed as a one-problem batch;
 * ``tune_single(op, x_shape, y_shape)`` chooses the single-problem kernel
   variant and applies it with ``vp_set_kernel_variant``.
 
@@ -26,7 +26,7 @@ import torch
 
 from . import _lib
 
-BATCH_CANDIDATES = {"forward": [1, 2], "backward": [4, 3]}
+BATCH_CANDIDATES = {"forward": [1], "backward": [6, 4]}
 SINGLE_CANDIDATES = {"forward": [1, 2, 3, 4], "backward": [6, 4, 1, 3]}
 TUNE_ANGLES = 90
 
@@ -73,6 +73,8 @@ def batch_variant(op: str, side: int, n_ang: int, device="cuda") -> int:
     cache = _load()
     if key in cache:
         return int(cache[key]["variant"])
+    if len(BATCH_CANDIDATES[op]) == 1:
+        return BATCH_CANDIDATES[op][0]
     from .batch import Batch
 
     n = min(n_ang, TUNE_ANGLES)

@@ -154,7 +154,9 @@ __device__ __forceinline__ void run_bwd_runs_item(const BatchDesc& d, int stage,
   signal_done(ctr);
 }
 
-__global__ void __launch_bounds__(BATCH_THREADS)
+// 7 resident blocks per SM (72 registers), the occupancy of the
+// single-problem run adjoint; the few spilled values are item bookkeeping.
+__global__ void __launch_bounds__(BATCH_THREADS, 7)
     batch_kernel(const BatchDesc* __restrict__ descs, int ndesc, long long total,
                  unsigned long long* __restrict__ next, unsigned* __restrict__ counters,
                  int* __restrict__ error) {

@@ -78,6 +78,11 @@ class Request:
         return _F32 * (3 * nv + 3 * ns)  # x, s, p; b, r, q
 
 
+def _zero(ts) -> None:
+    if ts:
+        torch._foreach_zero_(ts)
+
+
 @dataclass
 class _State:
     req: Request
@@ -185,8 +190,8 @@ class ReconstructionServer:
         cgls_new = [st for st in self.active if st.req.method == "cgls" and st.fresh]
 
         # outputs are accumulated into: clear them first
-        torch._foreach_zero_([st.bufs["ax"] for st in sirt_run] + [st.bufs["R"] for st in sirt_new]
-                             + [st.bufs["q"] for st in cgls_run])
+        _zero([st.bufs["ax"] for st in sirt_run] + [st.bufs["R"] for st in sirt_new]
+              + [st.bufs["q"] for st in cgls_run])
         fwd = self._forward_problems()
         if fwd:
             self._plan(("F",) + key, fwd).run()
@@ -209,8 +214,8 @@ class ReconstructionServer:
             b["x"].add_(alpha * b["p"])
             b["r"].sub_(alpha * b["q"])
 
-        torch._foreach_zero_([st.bufs["g"] for st in sirt_run] + [st.bufs["C"] for st in sirt_new]
-                             + [st.bufs["s"] for st in cgls_run + cgls_new])
+        _zero([st.bufs["g"] for st in sirt_run] + [st.bufs["C"] for st in sirt_new]
+              + [st.bufs["s"] for st in cgls_run + cgls_new])
         bwd = self._backward_problems()
         if bwd:
             self._plan(("B",) + key, bwd).run()

@@ -441,7 +441,9 @@ def e2e_leg(args, vp, x_dev, ang_np, dev):
             "d2h_bytes_per_step": sino + vol,
             "path": "voxelproj_gb300.forward(x, angles, y) then backward(y, angles, x') with "
                     "pinned CPU tensors (inputs and accumulate-into containers copied in, "
-                    "results copied out, every step)"}
+                    "results copied out, every step; z_order 0 host arrays go through "
+                    "vp_forward_z0_host / vp_backward_z0_host, which overlap the copies "
+                    "with the kernels)"}
 
 
 def main():

@@ -68,6 +68,8 @@ extern "C" {
 #define VP_FLAG_TRIG_PRECISE 1  /* accurate sincosf / IEEE division for the per-angle
                                    constants; default is the hardware approximations
                                    that the reference's --use_fast_math build uses */
+#define VP_FLAG_OVERWRITE 2     /* out = result instead of out += result; the output
+                                   is not read (host-buffer entry points only) */
 
 /* Library version, major*10000 + minor*100 + patch. */
 VP_API int vp_version(void);
@@ -195,6 +197,28 @@ VP_API int64_t vp_batch_work_items(const vp_batch_plan* plan);
  * wrong).  Stays set for the plan's lifetime once raised. */
 VP_API int vp_batch_error(vp_batch_plan* plan, int* error);
 VP_API int vp_batch_destroy(vp_batch_plan* plan);
+
+/* ---- Host buffers --------------------------------------------------------
+ * y (+)= A x and x (+)= A^T y, z_order 0, with x and y in host memory (any
+ * memory cudaMemcpyDefault can address); angles in host or device memory.
+ * Dims as for vp_forward_z0 / vp_backward_z0.  The library stages the arrays
+ * through device buffers of its own pool and overlaps the copies with the
+ * kernels: the forward starts on the first volume rows while the rest are in
+ * flight, the adjoint sends finished voxel rows back while later rows are
+ * computed.  Page-locked host buffers make the copies asynchronous; pageable
+ * ones work with less overlap.  The call is asynchronous on `stream`: the
+ * host output is complete when the stream is, and the host arrays must not
+ * be modified before then.  Same results as the device entry points with the
+ * same kernel variant, and the same per-slab summation; flags may add
+ * VP_FLAG_OVERWRITE.  No counterpart in the reference, whose Python wrappers
+ * copy the whole input in, project, and copy the result out one after
+ * another (voxelproj/wrappers.py:10-25, :57-73). */
+VP_API int vp_forward_z0_host(const float* x, int64_t x0, int64_t x1, int64_t x2, float* y,
+                              int64_t y0, int64_t y1, int64_t y2, const float* angles,
+                              int64_t n_angles, int flags, void* stream);
+VP_API int vp_backward_z0_host(const float* y, int64_t y0, int64_t y1, int64_t y2, float* x,
+                               int64_t x0, int64_t x1, int64_t x2, const float* angles,
+                               int64_t n_angles, int flags, void* stream);
 
 /* z_order dispatch, as voxelproj.wrappers.forward/backward select a kernel by
  * z_order (voxelproj/wrappers.py:44-47, :92-95); dims as for the

@@ -48,7 +48,10 @@ def test_batch_matches_single_problem_calls(vf, vb):
     b.run()
     torch.cuda.synchronize()
     assert not b.error()
-    _lib.LIB.vp_set_kernel_variant(1, vb)
+    # the single-problem kernels with the batch's bodies: forward 1, adjoint
+    # runs (6) or 2x2 blocks (4)
+    _lib.LIB.vp_set_kernel_variant(0, 1)
+    _lib.LIB.vp_set_kernel_variant(1, vb or 6)
     try:
         for c, (yo, xo) in zip(cases, outs):
             SY, SX, H, n, PX = c["geom"]
@@ -63,6 +66,7 @@ def test_batch_matches_single_problem_calls(vf, vb):
             Ax = oracle.forward(c["x"], c["ang"], PX, 0)
             assert rel_err(yo.cpu().numpy() - c["y0"], Ax) <= tol.ref_vs_fp64(max(SY, SX, PX))
     finally:
+        _lib.LIB.vp_set_kernel_variant(0, 0)
         _lib.LIB.vp_set_kernel_variant(1, 0)
     b.close()
 
@@ -84,15 +88,21 @@ def test_batch_stages_on_large_problems():
     b.run()  # runs accumulate: every output is now twice the operator
     torch.cuda.synchronize()
     assert not b.error()
-    for x, y, yo, xo, a in refs:
-        ys = torch.zeros_like(yo)
-        xs = torch.zeros_like(xo)
-        for _ in range(2):
-            vp._CU.forward_z0(x, ys, a)
-            vp._CU.backward_z0(y, xs, a)
-        torch.cuda.synchronize()
-        assert torch.equal(yo, ys)
-        assert torch.equal(xo, xs)
+    _lib.LIB.vp_set_kernel_variant(0, 1)  # the single-problem kernels with the batch's bodies
+    _lib.LIB.vp_set_kernel_variant(1, 6)
+    try:
+        for x, y, yo, xo, a in refs:
+            ys = torch.zeros_like(yo)
+            xs = torch.zeros_like(xo)
+            for _ in range(2):
+                vp._CU.forward_z0(x, ys, a)
+                vp._CU.backward_z0(y, xs, a)
+            torch.cuda.synchronize()
+            assert torch.equal(yo, ys)
+            assert torch.equal(xo, xs)
+    finally:
+        _lib.LIB.vp_set_kernel_variant(0, 0)
+        _lib.LIB.vp_set_kernel_variant(1, 0)
     b.close()
 
 

@@ -50,14 +50,14 @@ DUMMY = ctypes.c_void_p(0x1000)  # never dereferenced: validation fails first
 
 
 @pytest.mark.parametrize("fn", ["vp_forward_z0", "vp_backward_z0", "vp_forward_z2",
-                                "vp_backward_z2"])
+                                "vp_backward_z2", "vp_forward_z0_host", "vp_backward_z0_host"])
 def test_validation_errors_without_gpu(fn):
     f = getattr(_lib.LIB, fn)
     good = (4, 5, 6)
     # negative dimension
     assert f(DUMMY, -1, 5, 6, DUMMY, *good, DUMMY, 10, 0, None) == _lib.VP_ERR_BAD_SHAPE
     # too few angles for the sinogram's angle extent (7 angles, 6 given)
-    y_dims = (7, 5, 6) if fn.endswith("z0") else (6, 7, 5)
+    y_dims = (7, 5, 6) if "z0" in fn else (6, 7, 5)
     args = (DUMMY, *good, DUMMY, *y_dims) if "forward" in fn else (DUMMY, *y_dims, DUMMY, *good)
     assert f(*args, DUMMY, 6, 0, None) == _lib.VP_ERR_ANGLES
     # unknown flag bits
@@ -68,6 +68,9 @@ def test_validation_errors_without_gpu(fn):
     # empty problems succeed without touching the device
     assert f(None, 0, 0, 0, None, 0, 0, 0, None, 0, 0, None) == _lib.VP_OK
     assert f(DUMMY, 4, 5, 0, DUMMY, 4, 5, 0, DUMMY, 10, 0, None) == _lib.VP_OK
+    # VP_FLAG_OVERWRITE belongs to the host-buffer entry points only
+    ow = f(DUMMY, 4, 5, 0, DUMMY, 4, 5, 0, DUMMY, 10, _lib.VP_FLAG_OVERWRITE, None)
+    assert ow == (_lib.VP_OK if fn.endswith("_host") else _lib.VP_ERR_BAD_FLAGS)
 
 
 def test_dispatch_rejects_bad_z_order():

@@ -1,0 +1,139 @@
+"""Host-buffer entry points (vp_forward_z0_host / vp_backward_z0_host) and the
+wrappers' host path: the same operator as the device entry points, with the
+copies overlapped; several slabs, ragged row splits, both output modes."""
+
+from __future__ import annotations
+
+import numpy as np
+import pytest
+import torch
+
+import voxelproj_gb300 as vp
+from oracle import oracle
+from tests import tolerances as tol
+from tests.common import lin, rel_err, seeded
+from voxelproj_gb300 import _lib
+
+pytestmark = pytest.mark.gpu
+
+# (SY, SX, H, n_ang, PX): one slab; several forward slabs and adjoint row
+# slabs with a ragged last one (SY not a multiple of the slab rows); heights
+# of one float4 chunk and of two half-filled 256-height chunks
+GEOMS = [(20, 24, 8, 30, 28), (300, 260, 260, 12, 300), (61, 47, 132, 25, 50)]
+
+
+def _call(name, inp, out, ang, flags=0):
+    stream = torch.cuda.current_stream()
+    st = getattr(_lib.LIB, name)(inp.data_ptr(), *inp.shape, out.data_ptr(), *out.shape,
+                                 ang.data_ptr(), ang.numel(), flags, stream.cuda_stream)
+    _lib.check(st, name)
+    stream.synchronize()
+
+
+@pytest.mark.parametrize("geom", GEOMS, ids=lambda g: "x".join(map(str, g)))
+@pytest.mark.parametrize("pinned", [True, False])
+def test_host_entries_match_oracle_and_device_path(geom, pinned):
+    SY, SX, H, n, PX = geom
+    ang = lin(n, -0.3, 3.4)
+    x = torch.tensor(seeded((SY, SX, H), 1))
+    y = torch.tensor(seeded((n, PX, H), 2))
+    y0 = torch.tensor(seeded((n, PX, H), 3))
+    x0 = torch.tensor(seeded((SY, SX, H), 4))
+    if pinned:
+        x, y, y0, x0 = (t.pin_memory() for t in (x, y, y0, x0))
+    a_host = torch.tensor(ang)
+
+    yo = y0.clone()
+    _call("vp_forward_z0_host", x, yo, a_host)
+    xo = x0.clone()
+    _call("vp_backward_z0_host", y, xo, a_host)
+
+    n_ext = max(SY, SX, PX)
+    assert rel_err(yo.numpy() - y0.numpy(), oracle.forward(x.numpy(), ang, PX, 0)) <= \
+        tol.ref_vs_fp64(n_ext)
+    assert rel_err(xo.numpy() - x0.numpy(), oracle.backward(y.numpy(), ang, SY, SX, 0)) <= \
+        tol.ref_vs_fp64(n_ext)
+
+    # the device entry points: same operator, summed in another order
+    yd = y0.cuda()
+    vp._CU.forward_z0(x.cuda(), yd, a_host.cuda())
+    xd = x0.cuda()
+    vp._CU.backward_z0(y.cuda(), xd, a_host.cuda())
+    torch.cuda.synchronize()
+    assert rel_err(yo.numpy(), yd.cpu().numpy()) <= 1e-6
+    assert rel_err(xo.numpy(), xd.cpu().numpy()) <= 1e-6
+
+
+@pytest.mark.parametrize("geom", GEOMS[1:], ids=lambda g: "x".join(map(str, g)))
+def test_overwrite_mode_and_device_angles(geom):
+    """VP_FLAG_OVERWRITE: out = result, whatever the output held before;
+    angles may live on the device."""
+    SY, SX, H, n, PX = geom
+    ang = lin(n)
+    x = torch.tensor(seeded((SY, SX, H), 5)).pin_memory()
+    y = torch.tensor(seeded((n, PX, H), 6)).pin_memory()
+    a_dev = torch.tensor(ang, device="cuda")
+    yo = torch.full((n, PX, H), 7.0).pin_memory()
+    _call("vp_forward_z0_host", x, yo, a_dev, _lib.VP_FLAG_OVERWRITE)
+    xo = torch.full((SY, SX, H), -3.0)
+    _call("vp_backward_z0_host", y, xo, a_dev, _lib.VP_FLAG_OVERWRITE)
+    assert rel_err(yo.numpy(), oracle.forward(x.numpy(), ang, PX, 0)) <= tol.ref_vs_fp64(PX)
+    assert rel_err(xo.numpy(), oracle.backward(y.numpy(), ang, SY, SX, 0)) <= \
+        tol.ref_vs_fp64(max(SY, SX))
+
+
+def test_height_extents_differ():
+    """H = min(Hx, Hy): heights past the shorter array stay as they were
+    (accumulate) or become zero (overwrite)."""
+    SY, SX, n, PX = 18, 22, 14, 26
+    ang = lin(n)
+    x = torch.tensor(seeded((SY, SX, 12), 7))
+    y0 = torch.tensor(seeded((n, PX, 20), 8))
+    yo = y0.clone()
+    _call("vp_forward_z0_host", x, yo, torch.tensor(ang))
+    ref = oracle.forward(x.numpy(), ang, PX, 0)
+    assert rel_err(yo.numpy()[:, :, :12] - y0.numpy()[:, :, :12], ref) <= tol.REF_VS_FP64
+    np.testing.assert_array_equal(yo.numpy()[:, :, 12:], y0.numpy()[:, :, 12:])
+    yw = y0.clone()
+    _call("vp_forward_z0_host", x, yw, torch.tensor(ang), _lib.VP_FLAG_OVERWRITE)
+    assert not yw[:, :, 12:].any()
+    y = torch.tensor(seeded((n, PX, 8), 9))
+    xw = torch.full((SY, SX, 12), 5.0)
+    _call("vp_backward_z0_host", y, xw, torch.tensor(ang), _lib.VP_FLAG_OVERWRITE)
+    assert not xw[:, :, 8:].any()
+    assert rel_err(xw.numpy()[:, :, :8], oracle.backward(y.numpy(), ang, SY, SX, 0)) <= \
+        tol.REF_VS_FP64
+
+
+def test_wrappers_take_the_host_path_for_host_arrays():
+    SY, SX, H, n = 40, 40, 16, 33
+    ang = lin(n)
+    x = seeded((SY, SX, H), 10)
+    before = _lib.LIB.vp_launch_count()
+    y = vp.forward(x, ang, None)  # numpy in, numpy out, overwrite
+    assert isinstance(y, np.ndarray) and y.shape == (n, 40, H)
+    assert rel_err(y, oracle.forward(x, ang, 40, 0)) <= tol.REF_VS_FP64
+    # a float64 numpy container: accumulated into and returned
+    c = np.ones((SY, SX, H))
+    out = vp.backward(y, ang, c)
+    assert out is c and out.dtype == np.float64
+    assert rel_err(out - 1, oracle.backward(y, ang, SY, SX, 0)) <= tol.REF_VS_FP64
+    # a CPU tensor in, a CPU tensor back
+    t = vp.forward(torch.tensor(x), ang, (n, 40, H))
+    assert isinstance(t, torch.Tensor) and not t.is_cuda
+    assert rel_err(t.numpy(), y) <= 1e-6
+    assert _lib.LIB.vp_launch_count() > before
+
+
+def test_host_path_repeated_calls_reuse_pool():
+    """Back-to-back calls (buffers freed and re-taken on the stream) give the
+    same result every time."""
+    SY, SX, H, n, PX = 64, 64, 136, 40, 64
+    ang = torch.tensor(lin(n))
+    x = torch.tensor(seeded((SY, SX, H), 11)).pin_memory()
+    outs = []
+    for _ in range(3):
+        yo = torch.zeros(n, PX, H).pin_memory()
+        _call("vp_forward_z0_host", x, yo, ang)
+        outs.append(yo.clone())
+    assert torch.equal(outs[0], outs[1]) and torch.equal(outs[1], outs[2])

@@ -138,9 +138,9 @@ def test_weight_sum_single_voxel():
 # autotuner may pick any of them): sizes that are not multiples of the block
 # or run shape, degenerate angles, both signs of each step, several height
 # chunks.
-@pytest.mark.parametrize("variant", [1, 2, 3, 4, 5, 6])
+@pytest.mark.parametrize("variant", [1, 2, 3, 4, 5, 6, 7])
 @pytest.mark.parametrize("geom", [(23, 37, 132, 61, 50, "wide"), (9, 6, 8, 40, 11, "axes"),
-                                  (64, 64, 256, 96, 64, "rand")],
+                                  (64, 64, 256, 96, 64, "rand"), (30, 21, 260, 33, 40, "rand")],
                          ids=lambda g: "x".join(map(str, g[:5])) + g[5])
 def test_backward_variants(variant, geom):
     from voxelproj_gb300 import _lib
@@ -161,13 +161,14 @@ def test_backward_variants(variant, geom):
     assert err <= tol.ref_vs_fp64(max(SY, SX, PX))
 
 
-@pytest.mark.parametrize("variant", [1, 4, 6])
-def test_backward_variants_store_mode_via_z2(variant):
+@pytest.mark.parametrize("variant", [1, 4, 6, 7])
+@pytest.mark.parametrize("H", [36, 260])
+def test_backward_variants_store_mode_via_z2(variant, H):
     """z_order 2 with H >= 32 runs the z_order 0 kernel in store mode into
     scratch; the result must not depend on the scratch's prior content."""
     from voxelproj_gb300 import _lib
 
-    SY, SX, H, n, PX = 20, 26, 36, 30, 34
+    SY, SX, n, PX = 20, 26, 30, 34
     ang = lin(n)
     y = seeded((H, n, PX), 41)
     x0 = seeded((H, SY, SX), 42)
@@ -185,14 +186,15 @@ def test_backward_variants_store_mode_via_z2(variant):
     assert rel_err(outs[0] - x0, oracle.backward(y, ang, SY, SX, 2)) <= tol.ref_vs_fp64(PX)
 
 
-@pytest.mark.parametrize("variant", [1, 2, 3, 4])
+@pytest.mark.parametrize("variant", [1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12])
 @pytest.mark.parametrize("geom", [(23, 37, 132, 61, 50, "wide"), (9, 6, 8, 40, 11, "axes"),
-                                  (70, 64, 256, 96, 90, "rand")],
+                                  (70, 64, 256, 96, 90, "rand"), (30, 21, 260, 33, 40, "rand")],
                          ids=lambda g: "x".join(map(str, g[:5])) + g[5])
 def test_forward_variants(variant, geom):
     """Every kernel variant of the z_order 0 forward against the oracle:
-    bins per warp 4 / 8, warps of a block on neighbouring bins / angles, angle
-    counts that are not multiples of the group, degenerate angles."""
+    bins per warp 4 / 8, heights per lane 4 / 8 (with half-filled height
+    chunks), warps of a block on neighbouring bins / angles, angle counts that
+    are not multiples of the group, degenerate angles."""
     from voxelproj_gb300 import _lib
 
     SY, SX, H, n, PX, kind = geom
@@ -209,3 +211,28 @@ def test_forward_variants(variant, geom):
     err = rel_err(yo.cpu().numpy() - y0, oracle.forward(x, ang, PX, 0))
     print(f"\n[fwd variant {variant}] {geom}: A {err:.3e}")
     assert err <= tol.ref_vs_fp64(max(SY, SX, PX))
+
+
+@pytest.mark.parametrize("variant", [1, 5, 7, 8, 9, 12])
+@pytest.mark.parametrize("H", [36, 260])
+def test_forward_variants_store_mode_via_z2(variant, H):
+    """The forward's first slab launch writes the z_order 2 scratch in store
+    mode; repeated calls must not depend on the scratch's prior content."""
+    from voxelproj_gb300 import _lib
+
+    SY, SX, n, PX = 40, 26, 30, 34
+    ang = lin(n)
+    x = seeded((H, SY, SX), 43)
+    y0 = seeded((H, n, PX), 44)
+    _lib.LIB.vp_set_kernel_variant(0, variant)
+    try:
+        outs = []
+        for _ in range(2):
+            yo = torch.tensor(y0, device="cuda")
+            vp._CU.forward_z2(torch.tensor(x, device="cuda"), yo, torch.tensor(ang, device="cuda"))
+            torch.cuda.synchronize()
+            outs.append(yo.cpu().numpy())
+    finally:
+        _lib.LIB.vp_set_kernel_variant(0, 0)
+    np.testing.assert_array_equal(outs[0], outs[1])
+    assert rel_err(outs[0] - y0, oracle.forward(x, ang, PX, 2)) <= tol.ref_vs_fp64(PX)

@@ -13,7 +13,8 @@ grow with the largest extent N = max(SY, SX, PX):
   Measured: 1.7e-8..2.7e-8 * N at N = 50..512.
 * TRIG_REF vs FP64: the hardware sin/cos of the reference's fast-math build
   have an absolute error near 4e-7 on [-pi, pi], growing outside it.
-  Measured: 1.4e-7..2.8e-7 * N at N = 50..512, for angles up to 4*pi.
+  Measured: 1.4e-7..4.2e-7 * N at N = 40..512, for angles up to 4*pi
+  (the largest on a 30x21 volume with 40 bins and 33 random angles).
 * vs the reference's own kernels (golden fixtures, TRIG_REF): the parity
   target, 1e-5 relative, for A^T.  The reference's A marches rays with an
   accumulated float position.  It is itself off the exact operator by more
@@ -37,4 +38,4 @@ def precise_vs_fp64(n: int) -> float:
 
 def ref_vs_fp64(n: int) -> float:
     """Bound for TRIG_REF results on a geometry of largest extent n."""
-    return max(5e-6, 4e-7 * n)
+    return max(5e-6, 5e-7 * n)

@@ -44,6 +44,7 @@ class BatchProblem(ctypes.Structure):
 VP_NOALLOC_SCRATCH_BYTES = 64 << 20
 
 VP_FLAG_TRIG_PRECISE = 1
+VP_FLAG_OVERWRITE = 2
 
 _P = ctypes.c_void_p
 _I64 = ctypes.c_int64
@@ -73,6 +74,8 @@ SIGNATURES = {
     "vp_batch_work_items": (_I64, [_P]),
     "vp_batch_error": (_I, [_P, _P]),
     "vp_batch_destroy": (_I, [_P]),
+    "vp_forward_z0_host": (_I, [_P, _I64, _I64, _I64, _P, _I64, _I64, _I64, _P, _I64, _I, _P]),
+    "vp_backward_z0_host": (_I, [_P, _I64, _I64, _I64, _P, _I64, _I64, _I64, _P, _I64, _I, _P]),
     "vp_forward": (_I, [_P, _P, _P, _P, _P, _I64, _I, _I, _P]),
     "vp_backward": (_I, [_P, _P, _P, _P, _P, _I64, _I, _I, _P]),
 }

@@ -154,22 +154,22 @@ __global__ void __launch_bounds__(32 * BPB_WARPS)
 // saw no angle of its class leaves x untouched (in store mode the first launch
 // always writes).
 // ---------------------------------------------------------------------------
-template <int PASS>
-__global__ void __launch_bounds__(32 * BPR_WARPS)
+template <int PASS, int R>
+__global__ void __launch_bounds__(32 * BPR_WARPS, R == 8 ? 5 : 0)
     bp_z0_runs_kernel(const float* __restrict__ y, float* __restrict__ x,
-                      const float* __restrict__ angles, Geom g, int nrun_major, int nruns,
-                      int accumulate) {
+                      const float* __restrict__ angles, Geom g, int nrun_major, int run_base,
+                      int run_end, int accumulate) {
   __shared__ RunEntry tab[BPR_WARPS][BPR_CHUNK];
   __shared__ int alist[BPR_WARPS][BPR_LIST];
   const int lane = threadIdx.x;
   const int w = threadIdx.y;
-  const int run = blockIdx.x * BPR_WARPS + w;
-  if (run >= nruns) return;  // warp-uniform; all shared state is per warp
+  const int run = run_base + blockIdx.x * BPR_WARPS + w;
+  if (run >= run_end) return;  // warp-uniform; all shared state is per warp
   // PASS 0: run along x starting at (xi0, yi0); PASS 1: along y.
   const int xi0 = PASS == 0 ? (run % nrun_major) * RUN : run % nrun_major;
   const int yi0 = PASS == 0 ? run / nrun_major : (run / nrun_major) * RUN;
-  bp_runs_warp<PASS>(y, x, angles, g, xi0, yi0, (blockIdx.y * 32 + lane) * 4, accumulate,
-                     tab[w], alist[w]);
+  bp_runs_warp<PASS, R>(y, x, angles, g, xi0, yi0, blockIdx.y * 32 * R + lane * 4, accumulate,
+                        tab[w], alist[w]);
 }
 
 // ---------------------------------------------------------------------------
@@ -275,20 +275,29 @@ cudaError_t launch_bp_z0_block(const float* y, float* x, const float* angles, co
   return cudaGetLastError();
 }
 
+// Both class launches for the voxel rows [row_lo, row_hi); row_lo is a
+// multiple of RUN (class-1 runs span RUN rows).
+template <int R>
 cudaError_t launch_bp_z0_runs(const float* y, float* x, const float* angles, const Geom& g,
-                              cudaStream_t stream) {
+                              int row_lo, int row_hi, cudaStream_t stream) {
   dim3 block(32, BPR_WARPS);
-  const unsigned hchunks = ceil_div(g.H, 128);
+  const unsigned hchunks = ceil_div(g.H, 32 * R);
   const int nmaj0 = (int)ceil_div(g.SX, RUN);
-  const long long nruns0 = (long long)nmaj0 * g.SY;
-  bp_z0_runs_kernel<0><<<dim3(ceil_div(nruns0, BPR_WARPS), hchunks), block, 0, stream>>>(
-      y, x, angles, g, nmaj0, (int)nruns0, g.accumulate);
-  cudaError_t e = cudaGetLastError();
-  if (e != cudaSuccess) return e;
-  const long long nruns1 = (long long)g.SX * ceil_div(g.SY, RUN);
-  bp_z0_runs_kernel<1><<<dim3(ceil_div(nruns1, BPR_WARPS), hchunks), block, 0, stream>>>(
-      y, x, angles, g, g.SX, (int)nruns1, 1);
-  return cudaGetLastError();
+  const long long b0 = (long long)row_lo * nmaj0, e0 = (long long)row_hi * nmaj0;
+  if (e0 > b0) {
+    bp_z0_runs_kernel<0, R><<<dim3(ceil_div(e0 - b0, BPR_WARPS), hchunks), block, 0, stream>>>(
+        y, x, angles, g, nmaj0, (int)b0, (int)e0, g.accumulate);
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  const long long b1 = (long long)(row_lo / RUN) * g.SX;
+  const long long e1 = (long long)ceil_div(row_hi, RUN) * g.SX;
+  if (e1 > b1) {
+    bp_z0_runs_kernel<1, R><<<dim3(ceil_div(e1 - b1, BPR_WARPS), hchunks), block, 0, stream>>>(
+        y, x, angles, g, g.SX, (int)b1, (int)e1, 1);
+    return cudaGetLastError();
+  }
+  return cudaSuccess;
 }
 
 bool bp0_vec4(const float* y, const float* x, const Geom& g) {
@@ -298,14 +307,16 @@ bool bp0_vec4(const float* y, const float* x, const Geom& g) {
 
 int launches_backward_z0(const float* y, const float* x, const Geom& g) {
   const int v = kernel_variant(OP_BACKWARD_Z0);
-  return (bp0_vec4(y, x, g) && (v == 0 || v == 6)) ? 2 : 1;
+  return (bp0_vec4(y, x, g) && (v < 1 || v > 5)) ? 2 : 1;  // runs: two launches
 }
 
 // Variants: 1 = one voxel run per warp (bp_z0_kernel); 2 = 4x4 register
 // block; 3 = 4x2; 4 = 2x2 (accumulates in the reference's order, so its
 // results equal the reference's bit for bit); 5 = 8x2; 6 = runs along the
-// axis of smaller step, two launches (bp_z0_runs_kernel; the default when
-// heights come in float4, as the fastest).
+// axis of smaller step, two launches (bp_z0_runs_kernel); 7 = runs with 8
+// heights per lane (two float4, 128 heights apart; problems of at most 128
+// heights run 6).  The default when heights come in float4 is 7, the
+// fastest at 512^3 with 192 angles.
 cudaError_t launch_backward_z0(const float* y, float* x, const float* angles, const Geom& g,
                                cudaStream_t stream) {
   const bool vec4 = bp0_vec4(y, x, g);
@@ -316,7 +327,10 @@ cudaError_t launch_backward_z0(const float* y, float* x, const float* angles, co
       case 3: return launch_bp_z0_block<4, 2>(y, x, angles, g, stream);
       case 4: return launch_bp_z0_block<2, 2>(y, x, angles, g, stream);
       case 5: return launch_bp_z0_block<8, 2>(y, x, angles, g, stream);
-      default: return launch_bp_z0_runs(y, x, angles, g, stream);
+      case 6: return launch_bp_z0_runs<4>(y, x, angles, g, 0, g.SY, stream);
+      default:
+        if (g.H > 128) return launch_bp_z0_runs<8>(y, x, angles, g, 0, g.SY, stream);
+        return launch_bp_z0_runs<4>(y, x, angles, g, 0, g.SY, stream);
     }
   }
   const int R = vec4 ? 4 : 1;
@@ -327,6 +341,21 @@ cudaError_t launch_backward_z0(const float* y, float* x, const float* angles, co
   else
     bp_z0_kernel<1><<<grid, block, 0, stream>>>(y, x, angles, g);
   return cudaGetLastError();
+}
+
+int backward_z0_row_step(const float* y, const float* x, const Geom& g) {
+  const int v = kernel_variant(OP_BACKWARD_Z0);
+  return (bp0_vec4(y, x, g) && (v < 1 || v > 5)) ? RUN : 0;
+}
+
+cudaError_t launch_backward_z0_rows(const float* y, float* x, const float* angles,
+                                    const Geom& g, int row_lo, int row_hi,
+                                    cudaStream_t stream) {
+  if (row_lo == 0 && row_hi == g.SY) return launch_backward_z0(y, x, angles, g, stream);
+  if (backward_z0_row_step(y, x, g) == 0 || row_lo % RUN != 0) return cudaErrorInvalidValue;
+  const int v = kernel_variant(OP_BACKWARD_Z0);
+  if (v != 6 && g.H > 128) return launch_bp_z0_runs<8>(y, x, angles, g, row_lo, row_hi, stream);
+  return launch_bp_z0_runs<4>(y, x, angles, g, row_lo, row_hi, stream);
 }
 
 cudaError_t launch_backward_z2(const float* y, float* x, const float* angles, const Geom& g,

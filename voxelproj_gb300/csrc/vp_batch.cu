@@ -126,10 +126,12 @@ __device__ __forceinline__ void run_fwd_item(const BatchDesc& d, long long local
   const int p0 = (bg * BATCH_WARPS + w) * 4;
   const int h = (hc * 32 + lane) * 4;
   if (stage == 0) {
-    fp_z0_warp<4, 4>(d.in, d.out, d.angles, d.g, p0, a, h, y_lo, y_hi, 1, sm.cand[w]);
+    fp_z0_warp<4, 4>(d.in, d.out, d.angles, d.g, p0, a, h, row_slab(y_lo, y_hi, d.g.SX), 1,
+                     sm.cand[w]);
   } else {
     const StageWait wt{ctr - 1, (unsigned)(d.g.n_ang * d.units * BATCH_WARPS), error};
-    fp_z0_warp<4, 4>(d.in, d.out, d.angles, d.g, p0, a, h, y_lo, y_hi, 1, sm.cand[w], wt);
+    fp_z0_warp<4, 4>(d.in, d.out, d.angles, d.g, p0, a, h, row_slab(y_lo, y_hi, d.g.SX), 1,
+                     sm.cand[w], wt);
   }
   signal_done(ctr);
 }

@@ -25,18 +25,18 @@ struct RunEntry {
 // Fast path for advance pattern PAT: loads the W = 3 + popcount(PAT) window
 // bins with no predicates (the table phase routed windows that leave the
 // detector to the generic path), then applies the four voxels' weights.
-// p points at the window's first bin for this lane's heights; stride is the
-// signed distance between consecutive window bins.
-template <int PAT>
-__device__ __forceinline__ void run_window(float4 (&acc)[RUN], const float4 (&wv)[3],
-                                           const float* p, ptrdiff_t stride) {
+// p points at the window's first bin at this lane's first height (lh.s0);
+// stride is the signed distance between consecutive window bins.
+template <int PAT, int R>
+__device__ __forceinline__ void run_window(typename Vec<R>::T (&acc)[RUN], const float4 (&wv)[3],
+                                           const float* p, ptrdiff_t stride, const LaneH<R>& lh) {
   constexpr int o1 = (PAT & 1);
   constexpr int o2 = o1 + ((PAT >> 1) & 1);
   constexpr int o3 = o2 + ((PAT >> 2) & 1);
   constexpr int W = 3 + o3;
-  float4 win[W];
+  typename Vec<R>::T win[W];
 #pragma unroll
-  for (int u = 0; u < W; ++u) win[u] = __ldg(reinterpret_cast<const float4*>(p + u * stride));
+  for (int u = 0; u < W; ++u) win[u] = lh.load(p + u * stride);
   const float ws[12] = {wv[0].x, wv[0].y, wv[0].z, wv[0].w, wv[1].x, wv[1].y,
                         wv[1].z, wv[1].w, wv[2].x, wv[2].y, wv[2].z, wv[2].w};
   constexpr int off[RUN] = {0, o1, o2, o3};
@@ -58,26 +58,28 @@ __device__ __forceinline__ bool in_class(float phi, int trig) {
   return (PASS == 0) == (fabsf(c) <= fabsf(s));
 }
 
-// One warp: the run of class PASS starting at voxel (xi0, yi0), heights
-// [h, h + 4) of this lane.  tab (BPR_CHUNK entries) and alist (BPR_LIST
-// ints) are this warp's shared tables.  All 32 lanes must call it together.
-// wait() runs (by the whole warp) just before the outputs are written; with
-// Wait::coherent the read of the output bypasses L1.
-template <int PASS, class Wait = NoWait>
+// One warp: the run of class PASS starting at voxel (xi0, yi0), this lane's
+// heights from h (R = 4: [h, h + 4); R = 8: also [h + 128, h + 132)).  tab
+// (BPR_CHUNK entries) and alist (BPR_LIST ints) are this warp's shared
+// tables.  All 32 lanes must call it together.  wait() runs (by the whole
+// warp) just before the outputs are written; with Wait::coherent the read of
+// the output bypasses L1.
+template <int PASS, int R = 4, class Wait = NoWait>
 __device__ __forceinline__ void bp_runs_warp(const float* __restrict__ y, float* __restrict__ x,
                                              const float* __restrict__ angles, const Geom& g,
                                              int xi0, int yi0, int h, int accumulate,
                                              RunEntry* tab, int* alist,
                                              const Wait& wait = Wait()) {
+  using V = typename Vec<R>::T;
+  static_assert(R == 4 || R == 8, "heights per lane: 4 or 8");
   const int lane = threadIdx.x & 31;
-  const bool hv = h < g.H;
-  const int hs = hv ? h : 0;  // idle lanes read valid memory and never store
+  const LaneH<R> lh(h, g.H);
   const int dx = PASS == 0 ? 1 : 0;
   const int dy = PASS == 0 ? 0 : 1;
 
-  float4 acc[RUN];
+  V acc[RUN];
 #pragma unroll
-  for (int m = 0; m < RUN; ++m) acc[m] = vzero<float4>();
+  for (int m = 0; m < RUN; ++m) acc[m] = vzero<V>();
 
   const long long yrow = (long long)g.PX * g.Hy;
   int seen = 0;
@@ -146,17 +148,17 @@ __device__ __forceinline__ void bp_runs_warp(const float* __restrict__ y, float*
         const float4 wv[3] = {e.w[0], e.w[1], e.w[2]};
         const long long off =
             (long long)(unsigned)meta.x | ((long long)meta.y << 32);
-        const float* p = y + off + hs;
+        const float* p = y + off + lh.s0;
         const ptrdiff_t stride = meta.z;
         switch (meta.w) {
-          case 0: run_window<0>(acc, wv, p, stride); break;
-          case 1: run_window<1>(acc, wv, p, stride); break;
-          case 2: run_window<2>(acc, wv, p, stride); break;
-          case 3: run_window<3>(acc, wv, p, stride); break;
-          case 4: run_window<4>(acc, wv, p, stride); break;
-          case 5: run_window<5>(acc, wv, p, stride); break;
-          case 6: run_window<6>(acc, wv, p, stride); break;
-          case 7: run_window<7>(acc, wv, p, stride); break;
+          case 0: run_window<0, R>(acc, wv, p, stride, lh); break;
+          case 1: run_window<1, R>(acc, wv, p, stride, lh); break;
+          case 2: run_window<2, R>(acc, wv, p, stride, lh); break;
+          case 3: run_window<3, R>(acc, wv, p, stride, lh); break;
+          case 4: run_window<4, R>(acc, wv, p, stride, lh); break;
+          case 5: run_window<5, R>(acc, wv, p, stride, lh); break;
+          case 6: run_window<6, R>(acc, wv, p, stride, lh); break;
+          case 7: run_window<7, R>(acc, wv, p, stride, lh); break;
           default: {
             // generic path: three guarded loads per voxel, bins relative to
             // the window start (p), whose bin is r0 - dir
@@ -170,8 +172,9 @@ __device__ __forceinline__ void bp_runs_warp(const float* __restrict__ y, float*
 #pragma unroll
               for (int kk = 0; kk < 3; ++kk) {
                 const int bin = rr[m] + dir * (kk - 1);
-                const float4 v = ld_or_zero<float4>(p + (ptrdiff_t)(bin - base) * g.Hy,
-                                                    (unsigned)bin < (unsigned)g.PX);
+                const V v = (unsigned)bin < (unsigned)g.PX
+                                ? lh.load(p + (ptrdiff_t)(bin - base) * g.Hy)
+                                : vzero<V>();
                 acc[m] = f4_fma(ws[3 * m + kk], v, acc[m]);
               }
             }
@@ -185,18 +188,14 @@ __device__ __forceinline__ void bp_runs_warp(const float* __restrict__ y, float*
   }
 
   wait();
-  if (hv && (seen > 0 || !accumulate)) {
+  if (lh.v0 && (seen > 0 || !accumulate)) {  // a lane past H has no second half either
 #pragma unroll
     for (int m = 0; m < RUN; ++m) {
       const int xi = xi0 + m * dx;
       const int yi = yi0 + m * dy;
-      if (xi < g.SX && yi < g.SY) {
-        float4* px = reinterpret_cast<float4*>(x + ((size_t)yi * g.SX + xi) * g.Hx + h);
-        if constexpr (Wait::coherent)
-          store_out_coherent(px, acc[m]);
-        else
-          store_out(px, acc[m], accumulate);
-      }
+      if (xi < g.SX && yi < g.SY)
+        store_lane<R, Wait::coherent>(x + ((size_t)yi * g.SX + xi) * g.Hx, lh, acc[m],
+                                      accumulate);
     }
   }
 }

@@ -111,6 +111,46 @@ int kernel_variant(int op) {
 }
 }  // namespace vp
 
+// Host-buffer entry points (vp_host.cu).  VP_FLAG_OVERWRITE is accepted here
+// only.  An empty problem in overwrite mode still zeroes the output.
+namespace {
+
+cudaError_t zero_any(float* out, int64_t n, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  cudaMemPool_t pool;
+  cudaError_t e = private_pool(&pool);
+  if (e != cudaSuccess) return e;
+  void* z = nullptr;
+  const size_t bytes = (size_t)n * sizeof(float);
+  if ((e = cudaMallocFromPoolAsync(&z, bytes, pool, s)) != cudaSuccess) return e;
+  e = cudaMemsetAsync(z, 0, bytes, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(out, z, bytes, cudaMemcpyDefault, s);
+  const cudaError_t f = cudaFreeAsync(z, s);
+  return e != cudaSuccess ? e : f;
+}
+
+template <class Run>
+int host_entry(const float* x, int64_t x0, int64_t x1, int64_t x2, const float* y, int64_t y0,
+               int64_t y1, int64_t y2, float* out, int64_t out_elems, const float* angles,
+               int64_t n_angles, int flags, void* stream, Run run) {
+  const bool overwrite = (flags & VP_FLAG_OVERWRITE) != 0;
+  vp::Geom g;
+  bool empty = false;
+  if (int s = make_geom(x, x0, x1, x2, y, y0, y1, y2, angles, n_angles,
+                        flags & ~VP_FLAG_OVERWRITE, &g, &empty))
+    return s;
+  const cudaStream_t st = (cudaStream_t)stream;
+  if (empty) return overwrite ? finish(zero_any(out, out_elems, st), 0) : VP_OK;
+  g.accumulate = overwrite ? 0 : 1;
+  cudaMemPool_t pool;
+  cudaError_t e = private_pool(&pool);
+  int launches = 0;
+  if (e == cudaSuccess) e = run(g, pool, st, &launches);
+  return finish(e, launches);
+}
+
+}  // namespace
+
 extern "C" {
 
 int vp_set_kernel_variant(int op, int variant) {
@@ -157,7 +197,7 @@ int vp_forward_z0(const float* x, int64_t x0, int64_t x1, int64_t x2, float* y, 
     return s;
   if (empty) return VP_OK;
   return finish(vp::launch_forward_z0(x, y, angles, g, (cudaStream_t)stream),
-                vp::launches_forward_z0(g));
+                vp::launches_forward_z0(x, y, g));
 }
 
 int vp_backward_z0(const float* y, int64_t y0, int64_t y1, int64_t y2, float* x, int64_t x0,
@@ -170,6 +210,24 @@ int vp_backward_z0(const float* y, int64_t y0, int64_t y1, int64_t y2, float* x,
   if (empty) return VP_OK;
   return finish(vp::launch_backward_z0(y, x, angles, g, (cudaStream_t)stream),
                 vp::launches_backward_z0(y, x, g));
+}
+
+int vp_forward_z0_host(const float* x, int64_t x0, int64_t x1, int64_t x2, float* y, int64_t y0,
+                       int64_t y1, int64_t y2, const float* angles, int64_t n_angles, int flags,
+                       void* stream) {
+  return host_entry(x, x0, x1, x2, y, y0, y1, y2, y, y0 * y1 * y2, angles, n_angles, flags,
+                    stream, [&](const vp::Geom& g, cudaMemPool_t pool, cudaStream_t s, int* n) {
+                      return vp::forward_z0_host(x, y, angles, g, pool, s, n);
+                    });
+}
+
+int vp_backward_z0_host(const float* y, int64_t y0, int64_t y1, int64_t y2, float* x, int64_t x0,
+                        int64_t x1, int64_t x2, const float* angles, int64_t n_angles, int flags,
+                        void* stream) {
+  return host_entry(x, x0, x1, x2, y, y0, y1, y2, x, x0 * x1 * x2, angles, n_angles, flags,
+                    stream, [&](const vp::Geom& g, cudaMemPool_t pool, cudaStream_t s, int* n) {
+                      return vp::backward_z0_host(y, x, angles, g, pool, s, n);
+                    });
 }
 
 size_t vp_z2_workspace_bytes(int64_t x0, int64_t x1, int64_t x2, int64_t y0, int64_t y1,

@@ -178,7 +178,25 @@ __device__ __forceinline__ float vzero<float>() { return 0.0f; }
 template <>
 __device__ __forceinline__ float4 vzero<float4>() { return make_float4(0.f, 0.f, 0.f, 0.f); }
 
-// Float vector of R heights per lane (R = 1 or 4) and a guarded load of it.
+// Eight heights of one lane in two float4: [h, h + 4) and [h + 128, h + 132),
+// so that each of the warp's two loads covers 512 contiguous bytes.
+struct float4x2 {
+  float4 a, b;
+};
+constexpr int kSecondHalf = 128;  // height offset of float4x2::b
+
+__device__ __forceinline__ float4x2 f4_fma(float w, const float4x2& v, float4x2 acc) {
+  acc.a = f4_fma(w, v.a, acc.a);
+  acc.b = f4_fma(w, v.b, acc.b);
+  return acc;
+}
+template <>
+__device__ __forceinline__ float4x2 vzero<float4x2>() {
+  return {vzero<float4>(), vzero<float4>()};
+}
+
+// Float vector of R heights per lane (R = 1, 4, or 8 as float4x2) and a
+// guarded load of it.
 template <int R>
 struct Vec;
 template <>
@@ -188,6 +206,35 @@ struct Vec<1> {
 template <>
 struct Vec<4> {
   using T = float4;
+};
+template <>
+struct Vec<8> {
+  using T = float4x2;
+};
+
+// Height offsets of one lane: R = 1 or 4 heights from h; R = 8 as float4x2
+// from h.  Lanes past H read offset 0 (always valid) and never store.
+template <int R>
+struct LaneH {
+  int h, s0, d1;  // first height; load offset of the first half, second minus first
+  bool v0, v1;    // halves inside [0, H)
+  __device__ __forceinline__ LaneH(int h_, int H) : h(h_) {
+    v0 = h < H;
+    s0 = v0 ? h : 0;
+    v1 = R == 8 && h + kSecondHalf < H;
+    d1 = (v1 ? h + kSecondHalf : 0) - s0;
+  }
+  // this lane's heights of a row, given q = row + s0
+  __device__ __forceinline__ typename Vec<R>::T load(const float* q) const {
+    if constexpr (R == 8) {
+      float4x2 v;
+      v.a = __ldg(reinterpret_cast<const float4*>(q));
+      v.b = __ldg(reinterpret_cast<const float4*>(q + d1));
+      return v;
+    } else {
+      return __ldg(reinterpret_cast<const typename Vec<R>::T*>(q));
+    }
+  }
 };
 
 template <typename V>
@@ -222,6 +269,26 @@ __device__ __forceinline__ void store_out(float* p, float v, int accumulate) {
 // not coherent across SMs.
 __device__ __forceinline__ void store_out_coherent(float4* p, float4 v) {
   *p = f4_add(__ldcg(p), v);
+}
+
+// Epilogue of one lane's heights of the output row that starts at p.  With
+// COHERENT the read of out bypasses L1 (accumulate only).
+template <int R, bool COHERENT = false>
+__device__ __forceinline__ void store_lane(float* p, const LaneH<R>& lh,
+                                           const typename Vec<R>::T& v, int accumulate) {
+  if constexpr (R == 8) {
+    if (lh.v0) {
+      float4* q = reinterpret_cast<float4*>(p + lh.h);
+      if constexpr (COHERENT) store_out_coherent(q, v.a); else store_out(q, v.a, accumulate);
+    }
+    if (lh.v1) {
+      float4* q = reinterpret_cast<float4*>(p + lh.h + kSecondHalf);
+      if constexpr (COHERENT) store_out_coherent(q, v.b); else store_out(q, v.b, accumulate);
+    }
+  } else if (lh.v0) {
+    auto* q = reinterpret_cast<typename Vec<R>::T*>(p + lh.h);
+    if constexpr (COHERENT && R == 4) store_out_coherent(q, v); else store_out(q, v, accumulate);
+  }
 }
 
 // Pre-store hook that does nothing (single-problem kernels).

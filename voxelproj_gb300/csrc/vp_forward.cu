@@ -27,39 +27,22 @@ namespace {
 
 using namespace detail;
 
-// ---------------------------------------------------------------------------
-// z_order 0: x (SY, SX, H), y (n_ang, PX, H); heights contiguous.
-// A warp owns angle a, KW consecutive bins and 32*R heights (lane <->
-// heights).  The voxels gathered are warp-uniform, so the warp enumerates
-// them cooperatively: lane j takes major line i0+j, computes its candidate
-// voxels and their bin weights into a per-warp shared list (offsets from a
-// warp prefix sum), then all lanes stream the list with broadcast reads,
-// FP0_UNROLL candidates at a time so their loads overlap, and accumulate
-// the KW bins in registers.  A candidate's three bins sit at run-relative
-// offsets q-2, q-1, q (q = round(xp) - p0 + 1), dispatched with a
-// warp-uniform switch.
-//
-// Cache locality: every angle touches the whole volume, so a launch is
-// restricted to one slab of rows [y_lo, y_hi) of the volume (all launches add
-// into y), and heights are the slowest grid axis.  Concurrently running
-// blocks then share one slab x one 128-height chunk, a few tens of MB that
-// stay in L2 across all angles instead of being re-read from HBM per angle.
-// With AGROUP the four warps of a block take four consecutive angles of the
-// same bins: their voxel strips largely coincide, so one warp's loads are L1
-// hits for the others.
-// ---------------------------------------------------------------------------
-template <int R, int KW, bool AGROUP>
+// z_order 0 kernel: one fp_z0_warp per warp (the design is described in
+// vp_fp_z0.cuh).  Blocks of FP0_WARPS warps take neighbouring bin runs of one
+// angle, or with AGROUP one bin run of neighbouring angles; blockIdx.z is the
+// height chunk of 32 * R heights.
+template <int R, int KW, bool AGROUP, int UN>
 __global__ void __launch_bounds__(32 * FP0_WARPS)
     fp_z0_kernel(const float* __restrict__ x, float* __restrict__ y,
-                 const float* __restrict__ angles, Geom g, int a_base, int y_lo, int y_hi,
+                 const float* __restrict__ angles, Geom g, int a_base, Slab slab,
                  int accumulate) {
   __shared__ float4 cand[FP0_WARPS][32 * Fp0Cap<KW>::value];
   const int lane = threadIdx.x;
   const int w = threadIdx.y;
   const int p0 = (AGROUP ? blockIdx.x : blockIdx.x * FP0_WARPS + w) * KW;
   const int a = a_base + (AGROUP ? blockIdx.y * FP0_WARPS + w : blockIdx.y);
-  const int h = (blockIdx.z * 32 + lane) * R;
-  fp_z0_warp<R, KW>(x, y, angles, g, p0, a, h, y_lo, y_hi, accumulate, cand[w]);
+  const int h = blockIdx.z * 32 * R + lane * (R == 8 ? 4 : R);
+  fp_z0_warp<R, KW, UN>(x, y, angles, g, p0, a, h, slab, accumulate, cand[w]);
 }
 
 // ---------------------------------------------------------------------------
@@ -133,45 +116,122 @@ constexpr int kMaxGridYZ = 65535;
 
 }  // namespace
 
-// Rows per slab: about 32 MB of one 128-height chunk of the volume.
-int fp0_slab_rows(const Geom& g) {
-  const long long bytes_per_row = (long long)g.SX * 128 * 4;
-  long long rows = (32ll << 20) / (bytes_per_row > 0 ? bytes_per_row : 1);
+// Launch configuration of a forward variant for one problem.
+struct Fp0Config {
+  int R;          // heights per lane: 1, 4, or 8 (two float4)
+  int KW;         // bins per warp
+  bool agroup;    // warps of a block on neighbouring angles
+  int un;         // candidates loaded together
+  int slab_mb;    // volume bytes of one height chunk per slab launch
+  bool cls;       // class slabs (rows for one angle class, columns for the other)
+};
+
+// Variants: 1 = 4 bins per warp, 4 heights per lane, warps of a block on
+// neighbouring bins; 2 = 8 bins; 3 = 4 bins, warps of a block on
+// neighbouring angles; 4 = 8 bins, neighbouring angles; 5 = 4 bins, 8
+// heights per lane, 2 candidates in flight; 6 = as 5 with 4 in flight;
+// 7 = as 5 with 64 MB slabs; 8 = 8 bins, 8 heights per lane; 9 / 10 / 11 =
+// as 5 with class slabs of 32 / 64 / 128 MB (10 is the default); 12 = as 1
+// with class slabs of 32 MB.  Heights not in float4 run the scalar form of the same bin layout;
+// 8-height variants on problems of at most 128 heights run the 4-height form.
+Fp0Config fp0_config(const Geom& g, bool vec4, int variant) {
+  Fp0Config c{vec4 ? 4 : 1, 4, false, FP0_UNROLL, 32, false};
+  if (variant == 0) variant = 10;  // the default (fastest at 512^3 with 192 angles)
+  switch (variant) {
+    case 2: c.KW = 8; break;
+    case 3: c.agroup = true; break;
+    case 4: c.KW = 8; c.agroup = true; break;
+    case 5: c.R = 8; c.un = 2; break;
+    case 6: c.R = 8; break;
+    case 7: c.R = 8; c.un = 2; c.slab_mb = 64; break;
+    case 8: c.R = 8; c.KW = 8; c.un = 2; break;
+    case 9: c.R = 8; c.un = 2; c.cls = true; break;
+    case 10: c.R = 8; c.un = 2; c.cls = true; c.slab_mb = 64; break;
+    case 11: c.R = 8; c.un = 2; c.cls = true; c.slab_mb = 128; break;
+    case 12: c.cls = true; break;
+    default: break;
+  }
+  if (c.R == 8 && (!vec4 || g.H <= 128)) {
+    c.R = vec4 ? 4 : 1;
+    c.un = FP0_UNROLL;
+  }
+  return c;
+}
+
+// Slab launches of a call.  A row slab holds about slab_mb of one height
+// chunk (at least 128 heights) of the volume, in whole rows (at least 8); a
+// class slab's rows and columns together hold about as much, rows and
+// columns split evenly over the slabs.
+long long fp0_chunk_bytes(const Geom& g, const Fp0Config& c) {
+  const long long chunk_h = 32 * c.R > 128 ? 32 * c.R : 128;
+  return (long long)g.SY * g.SX * chunk_h * 4;
+}
+
+int fp0_slab_rows(const Geom& g, const Fp0Config& c) {
+  const long long bytes_per_row = fp0_chunk_bytes(g, c) / (g.SY > 0 ? g.SY : 1);
+  long long rows = ((long long)c.slab_mb << 20) / (bytes_per_row > 0 ? bytes_per_row : 1);
   if (rows < 8) rows = 8;
   return (int)(rows < g.SY ? rows : g.SY);
 }
 
-int launches_forward_z0(const Geom& g) {
-  const int rows = fp0_slab_rows(g);
-  const int v = kernel_variant(OP_FORWARD_Z0);
-  const long long per = (v == 3 || v == 4) ? (long long)kMaxGridYZ * FP0_WARPS : kMaxGridYZ;
-  return (int)(ceil_div(g.SY, rows) * ceil_div(g.n_ang, per));
+int fp0_slabs(const Geom& g, const Fp0Config& c) {
+  if (!c.cls) return (int)ceil_div(g.SY, fp0_slab_rows(g, c));
+  const long long budget = (long long)c.slab_mb << 20;
+  long long n = (2 * fp0_chunk_bytes(g, c) + budget - 1) / budget;
+  const long long nmax = ((g.SX < g.SY ? g.SX : g.SY) + 7) / 8;  // >= 8 lines per slab
+  if (n > nmax) n = nmax;
+  return (int)(n < 1 ? 1 : n);
+}
+
+Slab fp0_slab(const Geom& g, const Fp0Config& c, int k, int n) {
+  if (!c.cls) {
+    const int rows = fp0_slab_rows(g, c);
+    const int y_lo = k * rows;
+    return row_slab(y_lo, y_lo + rows < g.SY ? y_lo + rows : g.SY, g.SX);
+  }
+  const int wy = (g.SY + n - 1) / n;
+  const int wx = (g.SX + n - 1) / n;
+  const int y_lo = k * wy < g.SY ? k * wy : g.SY;
+  const int x_lo = k * wx < g.SX ? k * wx : g.SX;
+  return Slab{y_lo, y_lo + wy < g.SY ? y_lo + wy : g.SY,
+              x_lo, x_lo + wx < g.SX ? x_lo + wx : g.SX, 0, g.SY};
+}
+
+bool fp0_vec4(const float* x, const float* y, const Geom& g) {
+  return (g.Hx % 4 == 0) && (g.Hy % 4 == 0) &&
+         ((reinterpret_cast<uintptr_t>(x) | reinterpret_cast<uintptr_t>(y)) & 15) == 0;
+}
+
+int launches_forward_z0(const float* x, const float* y, const Geom& g) {
+  const Fp0Config c = fp0_config(g, fp0_vec4(x, y, g), kernel_variant(OP_FORWARD_Z0));
+  const long long per = c.agroup ? (long long)kMaxGridYZ * FP0_WARPS : kMaxGridYZ;
+  return (int)(fp0_slabs(g, c) * ceil_div(g.n_ang, per));
 }
 
 int launches_forward_z2(const Geom& g) {
   return (int)ceil_div(g.n_ang, (long long)kMaxGridYZ * FP2_WARPS);
 }
 
-template <int R, int KW, bool AGROUP>
+// Slabs [k0, k1) of the configuration's nslabs.
+template <int R, int KW, bool AGROUP, int UN>
 cudaError_t launch_fp_z0(const float* x, float* y, const float* angles, const Geom& g,
-                         cudaStream_t stream) {
-  const int rows = fp0_slab_rows(g);
+                         const Fp0Config& c, int k0, int k1, cudaStream_t stream) {
+  const int nslabs = fp0_slabs(g, c);
   dim3 block(32, FP0_WARPS);
-  bool first = true;
   const long long angles_per_launch = AGROUP ? (long long)kMaxGridYZ * FP0_WARPS : kMaxGridYZ;
-  for (int y_lo = 0; y_lo < g.SY; y_lo += rows) {
-    const int y_hi = y_lo + rows < g.SY ? y_lo + rows : g.SY;
+  for (int k = k0; k < k1 && k < nslabs; ++k) {
+    const Slab slab = fp0_slab(g, c, k, nslabs);
     // the first slab applies the caller's mode; later slabs add to it
-    const int accumulate = first ? g.accumulate : 1;
-    first = false;
+    const int accumulate = k == 0 ? g.accumulate : 1;
     for (long long a_base = 0; a_base < g.n_ang; a_base += angles_per_launch) {
       const long long na = g.n_ang - a_base < angles_per_launch ? g.n_ang - a_base
                                                                  : angles_per_launch;
       const unsigned gx = AGROUP ? ceil_div(g.PX, KW) : ceil_div(g.PX, KW * FP0_WARPS);
       const unsigned gy = AGROUP ? ceil_div(na, FP0_WARPS) : (unsigned)na;
       dim3 grid(gx, gy, ceil_div(g.H, 32 * R));
-      fp_z0_kernel<R, KW, AGROUP><<<grid, block, 0, stream>>>(x, y, angles, g, (int)a_base, y_lo,
-                                                              y_hi, accumulate);
+      fp_z0_kernel<R, KW, AGROUP, UN><<<grid, block, 0, stream>>>(x, y, angles, g,
+                                                                  (int)a_base, slab,
+                                                                  accumulate);
       const cudaError_t e = cudaGetLastError();
       if (e != cudaSuccess) return e;
     }
@@ -180,26 +240,61 @@ cudaError_t launch_fp_z0(const float* x, float* y, const float* angles, const Ge
 }
 
 template <int R>
-cudaError_t launch_fp_z0_variant(const float* x, float* y, const float* angles, const Geom& g,
-                                 cudaStream_t stream, int variant) {
-  switch (variant) {
-    case 2: return launch_fp_z0<R, 8, false>(x, y, angles, g, stream);
-    case 3: return launch_fp_z0<R, 4, true>(x, y, angles, g, stream);
-    case 4: return launch_fp_z0<R, 8, true>(x, y, angles, g, stream);
-    default: return launch_fp_z0<R, 4, false>(x, y, angles, g, stream);
+cudaError_t launch_fp_z0_r(const float* x, float* y, const float* angles, const Geom& g,
+                           const Fp0Config& c, int k0, int k1, cudaStream_t stream) {
+  if (c.KW == 8) {
+    if (c.agroup) return launch_fp_z0<R, 8, true, FP0_UNROLL>(x, y, angles, g, c, k0, k1, stream);
+    return launch_fp_z0<R, 8, false, FP0_UNROLL>(x, y, angles, g, c, k0, k1, stream);
   }
+  if (c.agroup) return launch_fp_z0<R, 4, true, FP0_UNROLL>(x, y, angles, g, c, k0, k1, stream);
+  return launch_fp_z0<R, 4, false, FP0_UNROLL>(x, y, angles, g, c, k0, k1, stream);
 }
 
-// Variants: 1 = 4 bins per warp, warps of a block on neighbouring bins
-// (default, fastest at 512^3); 2 = 8 bins, neighbouring bins; 3 = 4 bins,
-// warps of a block on neighbouring angles; 4 = 8 bins, neighbouring angles.
+cudaError_t launch_fp_z0_config(const float* x, float* y, const float* angles, const Geom& g,
+                                const Fp0Config& c, int k0, int k1, cudaStream_t stream) {
+  if (c.R == 8) {
+    if (c.KW == 8) return launch_fp_z0<8, 8, false, 2>(x, y, angles, g, c, k0, k1, stream);
+    if (c.un == 2) return launch_fp_z0<8, 4, false, 2>(x, y, angles, g, c, k0, k1, stream);
+    return launch_fp_z0<8, 4, false, 4>(x, y, angles, g, c, k0, k1, stream);
+  }
+  if (c.R == 4) return launch_fp_z0_r<4>(x, y, angles, g, c, k0, k1, stream);
+  return launch_fp_z0_r<1>(x, y, angles, g, c, k0, k1, stream);
+}
+
 cudaError_t launch_forward_z0(const float* x, float* y, const float* angles, const Geom& g,
                               cudaStream_t stream) {
-  const bool vec4 = (g.Hx % 4 == 0) && (g.Hy % 4 == 0) &&
-                    ((reinterpret_cast<uintptr_t>(x) | reinterpret_cast<uintptr_t>(y)) & 15) == 0;
-  const int variant = kernel_variant(OP_FORWARD_Z0);
-  if (vec4) return launch_fp_z0_variant<4>(x, y, angles, g, stream, variant);
-  return launch_fp_z0_variant<1>(x, y, angles, g, stream, variant);
+  const Fp0Config c = fp0_config(g, fp0_vec4(x, y, g), kernel_variant(OP_FORWARD_Z0));
+  return launch_fp_z0_config(x, y, angles, g, c, 0, 1 << 30, stream);
+}
+
+// Row-slab form of the selected variant, for volumes that arrive in row
+// order: slab k reads only rows [forward_z0_row_slab(k)).
+Fp0Config fp0_stream_config(const float* x, const float* y, const Geom& g) {
+  Fp0Config c = fp0_config(g, fp0_vec4(x, y, g), kernel_variant(OP_FORWARD_Z0));
+  c.cls = false;
+  return c;
+}
+
+int forward_z0_row_slabs(const float* x, const float* y, const Geom& g) {
+  return fp0_slabs(g, fp0_stream_config(x, y, g));
+}
+
+void forward_z0_row_slab(const float* x, const float* y, const Geom& g, int k, int* row_lo,
+                         int* row_hi) {
+  const Fp0Config c = fp0_stream_config(x, y, g);
+  const Slab s = fp0_slab(g, c, k, fp0_slabs(g, c));
+  *row_lo = s.y_lo;
+  *row_hi = s.y_hi;
+}
+
+cudaError_t launch_forward_z0_row_slab(const float* x, float* y, const float* angles,
+                                       const Geom& g, int k, cudaStream_t stream) {
+  return launch_fp_z0_config(x, y, angles, g, fp0_stream_config(x, y, g), k, k + 1, stream);
+}
+
+int forward_z0_row_slab_launches(const float* x, const float* y, const Geom& g) {
+  const Fp0Config c = fp0_stream_config(x, y, g);
+  return (int)ceil_div(g.n_ang, c.agroup ? (long long)kMaxGridYZ * FP0_WARPS : kMaxGridYZ);
 }
 
 cudaError_t launch_forward_z2(const float* x, float* y, const float* angles, const Geom& g,

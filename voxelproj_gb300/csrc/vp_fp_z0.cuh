@@ -32,27 +32,30 @@ __device__ __forceinline__ MinorRange minor_range(int i, float cent_major, float
 // ---------------------------------------------------------------------------
 // z_order 0: x (SY, SX, H), y (n_ang, PX, H); heights contiguous.
 // A warp owns angle a, KW consecutive bins and 32*R heights (lane <->
-// heights).  The voxels gathered are warp-uniform, so the warp enumerates
+// heights; with R = 8 a lane holds two float4, 128 heights apart).  The voxels gathered are warp-uniform, so the warp enumerates
 // them cooperatively: lane j takes major line i0+j, computes its candidate
 // voxels and their bin weights into a per-warp shared list (offsets from a
 // warp prefix sum), then all lanes stream the list with broadcast reads,
-// FP0_UNROLL candidates at a time so their loads overlap, and accumulate
+// UN candidates at a time so their loads overlap, and accumulate
 // the KW bins in registers.  A candidate's three bins sit at run-relative
 // offsets q-2, q-1, q (q = round(xp) - p0 + 1), dispatched with a
 // warp-uniform switch.
 //
 // Cache locality: every angle touches the whole volume, so a launch is
-// restricted to one slab of rows [y_lo, y_hi) of the volume (all launches add
-// into y), and heights are the slowest grid axis.  Concurrently running
-// blocks then share one slab x one 128-height chunk, a few tens of MB that
-// stay in L2 across all angles instead of being re-read from HBM per angle.
+// restricted to one slab of the volume (all launches add into y), and heights
+// are the slowest grid axis.  Concurrently running blocks then share one slab
+// x one height chunk, a few tens of MB that stay in L2 across all angles
+// instead of being re-read from HBM per angle.  With row slabs, angles whose
+// minor axis is y still walk every column per slab, mostly finding no
+// candidate in it; class slabs give those angles a block of columns instead,
+// so every warp walks only the major lines of its slab.
 // With AGROUP the four warps of a block take four consecutive angles of the
-// same bins: their voxel strips largely coincide, so one warp's loads are L1
-// hits for the others.
+// same bins, so their voxel strips overlap near the rotation centre (L1 hits);
+// at 512^3 this measured slower than neighbouring bins.
 // ---------------------------------------------------------------------------
 constexpr int FP0_WARPS = 4;
 constexpr int FP0_QBITS = 4;   // q in [0, KW + 1]
-constexpr int FP0_UNROLL = 4;  // candidates whose loads are in flight together
+constexpr int FP0_UNROLL = 4;  // candidates whose loads are in flight together (R <= 4)
 
 // >= max candidates per major line: floor((KW + 2b + margin) / sqrt(1/2)) + 1
 template <int KW>
@@ -85,15 +88,32 @@ __device__ __forceinline__ void scatter_q(V (&acc)[KW], const float4& e, const V
 #undef VP_Q_CASE
 }
 
-// One warp: angle a, bins [p0, p0 + KW), heights [h, h + R) of this lane,
-// volume rows [y_lo, y_hi).  cand is this warp's shared candidate list of
+// The part of the volume one launch (or one batch stage) gathers from.
+// Angles whose minor axis is x walk rows [y_lo, y_hi) (all columns); angles
+// whose minor axis is y walk columns [x_lo, x_hi) within rows [yy_lo, yy_hi).
+//   row slabs:   {y_lo, y_hi, 0, SX, y_lo, y_hi}  (one block of rows for all)
+//   class slabs: {y_lo, y_hi, x_lo, x_hi, 0, SY}  (rows for one class,
+//                                                  columns for the other)
+struct Slab {
+  int y_lo, y_hi;
+  int x_lo, x_hi;
+  int yy_lo, yy_hi;
+};
+
+__host__ __device__ inline Slab row_slab(int y_lo, int y_hi, int SX) {
+  return Slab{y_lo, y_hi, 0, SX, y_lo, y_hi};
+}
+
+// One warp: angle a, bins [p0, p0 + KW), this lane's heights from h (LaneH:
+// R = 8 is [h, h + 4) and [h + 128, h + 132)), the voxels of slab s.
+// UN candidates are loaded together.  cand is this warp's shared candidate list of
 // 32 * Fp0Cap<KW>::value entries.  All 32 lanes must call it together.
 // wait() runs (by the whole warp) just before the outputs are written; with
 // Wait::coherent the read of the output bypasses L1.
-template <int R, int KW, class Wait = NoWait>
+template <int R, int KW, int UN = FP0_UNROLL, class Wait = NoWait>
 __device__ __forceinline__ void fp_z0_warp(const float* __restrict__ x, float* __restrict__ y,
                                            const float* __restrict__ angles, const Geom& g,
-                                           int p0, int a, int h, int y_lo, int y_hi,
+                                           int p0, int a, int h, const Slab& s,
                                            int accumulate, float4* cand,
                                            const Wait& wait = Wait()) {
   using V = typename Vec<R>::T;
@@ -103,15 +123,15 @@ __device__ __forceinline__ void fp_z0_warp(const float* __restrict__ x, float* _
     wait();
     return;
   }
-  const bool hv = h < g.H;
+  const LaneH<R> lh(h, g.H);
 
   const AngleConst k = angle_const(__ldg(angles + a), g.trig);
   const bool minor_x = fabsf(k.c) >= fabsf(k.s);
   // major lines [maj_lo, maj_hi), minor indices [min_lo, min_hi], within the slab
-  const int maj_lo = minor_x ? y_lo : 0;
-  const int maj_hi = minor_x ? y_hi : g.SX;
-  const int min_lo = minor_x ? 0 : y_lo;
-  const int min_hi = minor_x ? g.SX - 1 : y_hi - 1;
+  const int maj_lo = minor_x ? s.y_lo : s.x_lo;
+  const int maj_hi = minor_x ? s.y_hi : s.x_hi;
+  const int min_lo = minor_x ? 0 : s.yy_lo;
+  const int min_hi = minor_x ? g.SX - 1 : s.yy_hi - 1;
   const float cent_major = minor_x ? g.ycent : g.xcent;
   const float cent_minor = minor_x ? g.xcent : g.ycent;
   const float sh_major = minor_x ? k.s : k.c;
@@ -122,7 +142,7 @@ __device__ __forceinline__ void fp_z0_warp(const float* __restrict__ x, float* _
   V acc[KW];
 #pragma unroll
   for (int b = 0; b < KW; ++b) acc[b] = vzero<V>();
-  const int hs = hv ? h : 0;  // idle lanes read row 0 (always valid) and never store
+  const float* xs = x + lh.s0;
 
   for (int i0 = maj_lo; i0 < maj_hi; i0 += 32) {
     const int i = i0 + lane;
@@ -158,17 +178,17 @@ __device__ __forceinline__ void fp_z0_warp(const float* __restrict__ x, float* _
       cand[start + t] = e;
     }
     __syncwarp();
-    for (int c0 = 0; c0 < total; c0 += FP0_UNROLL) {
-      float4 e[FP0_UNROLL];
-      V xv[FP0_UNROLL];
+    for (int c0 = 0; c0 < total; c0 += UN) {
+      float4 e[UN];
+      V xv[UN];
 #pragma unroll
-      for (int u = 0; u < FP0_UNROLL; ++u) {
+      for (int u = 0; u < UN; ++u) {
         e[u] = (c0 + u < total) ? cand[c0 + u] : make_float4(0.f, 0.f, 0.f, 0.f);
         const int vox = __float_as_int(e[u].w) >> FP0_QBITS;
-        xv[u] = __ldg(reinterpret_cast<const V*>(x + (size_t)vox * g.Hx + hs));
+        xv[u] = lh.load(xs + (size_t)vox * g.Hx);
       }
 #pragma unroll
-      for (int u = 0; u < FP0_UNROLL; ++u) {
+      for (int u = 0; u < UN; ++u) {
         if (c0 + u >= total) break;  // padding slots (warp-uniform)
         scatter_q<KW>(acc, e[u], xv[u], __float_as_int(e[u].w) & ((1 << FP0_QBITS) - 1));
       }
@@ -177,18 +197,11 @@ __device__ __forceinline__ void fp_z0_warp(const float* __restrict__ x, float* _
   }
 
   wait();
-  if (hv) {
 #pragma unroll
-    for (int b = 0; b < KW; ++b) {
-      const int p = p0 + b;
-      if (p < g.PX) {
-        V* py = reinterpret_cast<V*>(y + ((size_t)a * g.PX + p) * g.Hy + h);
-        if constexpr (Wait::coherent && R == 4)
-          store_out_coherent(py, acc[b]);
-        else
-          store_out(py, acc[b], accumulate);
-      }
-    }
+  for (int b = 0; b < KW; ++b) {
+    const int p = p0 + b;
+    if (p < g.PX)
+      store_lane<R, Wait::coherent>(y + ((size_t)a * g.PX + p) * g.Hy, lh, acc[b], accumulate);
   }
 }
 

@@ -40,9 +40,33 @@ cudaError_t forward_z2_transposed(const float* x, float* y, const float* angles,
 cudaError_t backward_z2_transposed(const float* y, float* x, const float* angles, const Geom& g,
                                    float* ws, cudaStream_t stream);
 
+// Streamed forms for host buffers.  Forward: the selected variant in row
+// slabs; slab k reads only volume rows [row_lo, row_hi), and launching slabs
+// 0..n-1 in order (slab 0 in g.accumulate's mode, later ones adding) gives
+// the full result.  Adjoint: voxel rows [row_lo, row_hi) alone, row_lo a
+// multiple of backward_z0_row_step() (0: rows cannot be split, launch
+// [0, SY) only).
+int forward_z0_row_slabs(const float* x, const float* y, const Geom& g);
+void forward_z0_row_slab(const float* x, const float* y, const Geom& g, int k, int* row_lo,
+                         int* row_hi);
+cudaError_t launch_forward_z0_row_slab(const float* x, float* y, const float* angles,
+                                       const Geom& g, int k, cudaStream_t stream);
+int forward_z0_row_slab_launches(const float* x, const float* y, const Geom& g);
+int backward_z0_row_step(const float* y, const float* x, const Geom& g);
+cudaError_t launch_backward_z0_rows(const float* y, float* x, const float* angles,
+                                    const Geom& g, int row_lo, int row_hi,
+                                    cudaStream_t stream);
+
+// Host-buffer projections (vp_host.cu): g.accumulate selects out += result
+// (1) or out = result (0); *launches is incremented by the kernels launched.
+cudaError_t forward_z0_host(const float* x_host, float* y_host, const float* angles,
+                            const Geom& g, cudaMemPool_t pool, cudaStream_t s, int* launches);
+cudaError_t backward_z0_host(const float* y_host, float* x_host, const float* angles,
+                             const Geom& g, cudaMemPool_t pool, cudaStream_t s, int* launches);
+
 // Kernel launches the forward launchers issue for a geometry (grids are
 // split past 65535 angle blocks).
-int launches_forward_z0(const Geom& g);
+int launches_forward_z0(const float* x, const float* y, const Geom& g);
 int launches_backward_z0(const float* y, const float* x, const Geom& g);
 int launches_forward_z2(const Geom& g);
 

@@ -94,7 +94,8 @@ int launches_z2(const Geom& g, bool forward) {
   Geom g0 = g;
   g0.H = g0.Hx = g0.Hy = (int)round4(g.H);
   static const float aligned[4] = {};
-  return 2 + (forward ? launches_forward_z0(g0) : launches_backward_z0(aligned, aligned, g0));
+  return 2 + (forward ? launches_forward_z0(aligned, aligned, g0)
+                      : launches_backward_z0(aligned, aligned, g0));
 }
 
 // x (Hx, SY, SX) -> xt (SY, SX, Hp); yt = A xt; y (Hy, n, PX) += yt^T.

@@ -20,6 +20,13 @@ Mirrors voxelproj/wrappers.py:10-122 of the reference:
 Beyond the reference: ``angles`` may also be a list or tuple (the reference
 accepted only arrays/tensors), non-contiguous inputs and outputs are handled
 instead of rejected or mis-written, and there is no 512-angle limit.
+
+Host arrays in z_order 0 (numpy or CPU tensors, with a host container or
+none) go through the library's host-buffer entry points
+(``vp_forward_z0_host`` / ``vp_backward_z0_host``), which overlap the
+copies to and from the GPU with the projection; the reference copies,
+projects and copies back one after another.  Page-locked CPU tensors
+(``tensor.pin_memory()``) give the most overlap.
 """
 
 from __future__ import annotations
@@ -27,6 +34,7 @@ from __future__ import annotations
 import numpy as np
 import torch
 
+from . import _CU, _lib
 from ._CU import backward_z0, backward_z2, forward_z0, forward_z2
 
 
@@ -83,6 +91,65 @@ def _kind(v):
     return "cuda", None
 
 
+def _host_out(out):
+    return out is None or isinstance(out, (tuple, np.ndarray)) or (
+        isinstance(out, torch.Tensor) and not out.is_cuda)
+
+
+def _host_array(v):
+    """Float32 C-contiguous host data of a numpy array or CPU tensor (no copy
+    when it already is one): (holder, address)."""
+    if isinstance(v, np.ndarray):
+        a = np.ascontiguousarray(v, dtype=np.float32)
+        return a, a.ctypes.data
+    t = v.detach().to(torch.float32).contiguous()
+    return t, t.data_ptr()
+
+
+def _host_call(fn_name, inp, out, angles, default_shape, kind):
+    """z_order 0 with host arrays through the host-buffer entry points."""
+    src, src_ptr = _host_array(inp)
+    if src.ndim != 3:
+        raise RuntimeError("Tensor must be 3D")
+    if isinstance(angles, torch.Tensor) and angles.is_cuda:
+        ang = angles.detach().to(torch.float32).reshape(-1).contiguous()
+        ang_ptr, n_ang = ang.data_ptr(), ang.numel()
+    else:
+        if isinstance(angles, torch.Tensor):
+            angles = angles.detach().cpu().numpy()
+        ang = np.ascontiguousarray(np.asarray(angles, dtype=np.float32).reshape(-1))
+        ang_ptr, n_ang = ang.ctypes.data, ang.size
+    flags = _CU._flags
+    if out is None or isinstance(out, tuple):
+        shape = default_shape if out is None else out
+        work = (np.empty(shape, np.float32) if kind == "numpy"
+                else torch.empty(shape, dtype=torch.float32))
+        result, flags = work, flags | _lib.VP_FLAG_OVERWRITE
+    else:
+        result = out
+        if isinstance(out, np.ndarray):
+            direct = (out.dtype == np.float32 and out.flags.c_contiguous
+                      and out.flags.writeable)
+            work = out if direct else np.ascontiguousarray(out, dtype=np.float32).copy()
+        else:
+            direct = out.dtype == torch.float32 and out.is_contiguous()
+            work = out if direct else out.to(torch.float32).contiguous()
+    if work.ndim != 3:
+        raise RuntimeError("out must be 3D")
+    work_ptr = work.ctypes.data if isinstance(work, np.ndarray) else work.data_ptr()
+    stream = torch.cuda.current_stream()
+    status = getattr(_lib.LIB, fn_name)(src_ptr, *src.shape, work_ptr, *work.shape, ang_ptr,
+                                        n_ang, flags, stream.cuda_stream)
+    _lib.check(status, fn_name[3:])
+    stream.synchronize()
+    if work is not result:
+        if isinstance(result, np.ndarray):
+            np.copyto(result, work)
+        else:
+            result.copy_(work)
+    return result
+
+
 def forward(x, angles, y, z_order=0, block_size=[8, 8, 8]):
     """Forward projection: returns y + A x (see module docstring)."""
     kind, device = _kind(x)
@@ -94,6 +161,8 @@ def forward(x, angles, y, z_order=0, block_size=[8, 8, 8]):
     project = {0: forward_z0, 2: forward_z2}
     shape = default_shape[z_order]
     fn = project[z_order]
+    if z_order == 0 and kind != "cuda" and _host_out(y):
+        return _host_call("vp_forward_z0_host", x, y, angles, shape, kind)
     x_gpu = _input_gpu(x)
     a_gpu = _angles_gpu(angles)
     y_gpu = gpu_array_with_default_shape(y, shape=shape)
@@ -112,6 +181,8 @@ def backward(y, angles, x, z_order=0, block_size=[8, 8, 8]):
     project = {0: backward_z0, 2: backward_z2}
     shape = default_shape[z_order]
     fn = project[z_order]
+    if z_order == 0 and kind != "cuda" and _host_out(x):
+        return _host_call("vp_backward_z0_host", y, x, angles, shape, kind)
     y_gpu = _input_gpu(y)
     a_gpu = _angles_gpu(angles)
     x_gpu = gpu_array_with_default_shape(x, shape=shape)

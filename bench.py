@@ -356,10 +356,14 @@ def run_ours(args, world, rank, local):
                  ("AT", 2): "bp_z2_kernel"}[(kern, z)]
         dur_s = (fwd_ms if kern == "A" else bwd_ms) / 1e3
         achieved = alg[kern] / dur_s / 1e9
-        traffic = None
+        # traffic per call of the operator (its slab / class launches together),
+        # the same unit as `achieved`, from the committed ncu capture
+        traffic, launches_per_call = None, None
         tr = read_json(ROOT / "profiles" / "traffic.json")
         if tr and tr.get("workload", {}).get("size") == S and tr["workload"].get("n_angles") == n:
-            traffic = tr.get("kernels", {}).get(kname, {}).get("dram_bytes_per_launch")
+            kt = tr.get("kernels", {}).get(kname, {})
+            traffic = kt.get("dram_bytes_per_call")
+            launches_per_call = kt.get("launches_per_call")
         nnz = weights_nnz(S, n, PX, ang_np)
         sms = torch.cuda.get_device_properties(dev).multi_processor_count
         clk = peaks.get("sm_max_mhz", 2070.0)
@@ -383,7 +387,9 @@ def run_ours(args, world, rank, local):
             "roofline": {"bound": "hbm", "kernel": kname, "achieved": round(achieved, 2),
                          "peak": hbm_peak, "peak_source": peak_note, "unit": "GB/s",
                          "frac": round(achieved / hbm_peak, 4), "traffic": traffic,
-                         "algorithmic_bytes": alg[kern]},
+                         "algorithmic_bytes": alg[kern],
+                         "per": "one %s call (%s kernel launches), CUDA events on its stream"
+                                % (kern, launches_per_call or "its")},
             "fma_roofline": {
                 "kernel": kname, "nonzero_weights": nnz,
                 "achieved": round(flops / dur_s / 1e12, 3), "unit": "TFLOP/s",

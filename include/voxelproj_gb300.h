@@ -154,8 +154,11 @@ VP_API int vp_forward_z2_noalloc(const float* x, int64_t x0, int64_t x1, int64_t
 
 /* ---- Batches -----------------------------------------------------------
  * Many problems of different sizes and angle counts, forward and adjoint
- * mixed, in ONE persistent kernel launch.  No counterpart in the reference,
- * which launches one kernel per call.
+ * mixed, in one persistent kernel launch per body present: the forward and
+ * the run adjoint with 4 or 8 heights per lane, so at most four launches
+ * however many problems.  Each body keeps its single-problem kernel's
+ * register budget.  No counterpart in the reference, which launches one
+ * kernel per call.
  *
  * A problem is in z_order 0 layout (x (SY, SX, H), y (n_ang, PX, H)) with
  * heights a multiple of 4 and 16-byte aligned buffers; its output is
@@ -168,10 +171,15 @@ VP_API int vp_forward_z2_noalloc(const float* x, int64_t x0, int64_t x1, int64_t
 typedef struct vp_batch_problem {
   int op;                 /* VP_OP_FORWARD or VP_OP_BACKWARD */
   int flags;              /* VP_FLAG_* as for the single-problem calls */
-  int variant;            /* 0 = default; forward: 1 (4 bins per warp, volume
-                             slabs); adjoint: 6 = runs in two angle classes
-                             (default), 4 = 2x2 voxel blocks (accumulates in the
-                             reference's order, bit-identical to it) */
+  int variant;            /* the single-problem kernel variant whose body,
+                             heights per lane and slabs the problem uses.
+                             Forward: 0 (default, = 10) or any variant with 4
+                             bins per warp on neighbouring bins (1, 5, 7, 9,
+                             10, 11, 12).  Adjoint: 0 / 7 = runs in two angle
+                             classes, 8 heights per lane past 128 heights
+                             (default); 6 = runs, 4 heights per lane; 4 = 2x2
+                             voxel blocks (accumulates in the reference's
+                             order, bit-identical to it) */
   int reserved;
   const float* in;        /* x for a forward problem, y for an adjoint one */
   float* out;             /* y for a forward problem, x for an adjoint one */
@@ -187,8 +195,9 @@ typedef struct vp_batch_plan vp_batch_plan;
  * device (the only device allocation); *plan receives the plan. */
 VP_API int vp_batch_create(const vp_batch_problem* problems, int count, vp_batch_plan** plan);
 /* Enqueues the whole batch on `stream`: a counter reset and one persistent
- * launch.  Allocates and synchronises nothing, so it can be captured in a
- * CUDA graph.  Runs of the same plan must not overlap on the GPU. */
+ * launch per body present.  Allocates and synchronises nothing, so it can be
+ * captured in a CUDA graph.  Runs of the same plan must not overlap on the
+ * GPU. */
 VP_API int vp_batch_run(vp_batch_plan* plan, void* stream);
 /* Work items of the plan (blocks' units of work). */
 VP_API int64_t vp_batch_work_items(const vp_batch_plan* plan);

@@ -1,4 +1,4 @@
-"""Batched persistent launch, CUDA-graph replay and the autotuner."""
+"""Batched persistent launches, CUDA-graph replay and the autotuner."""
 
 from __future__ import annotations
 
@@ -30,7 +30,7 @@ def _inputs(geoms, seed):
     return out
 
 
-@pytest.mark.parametrize("vf,vb", [(1, 4), (1, 6), (0, 0)])
+@pytest.mark.parametrize("vf,vb", [(1, 4), (1, 6), (0, 0), (10, 7), (5, 6), (12, 7)])
 def test_batch_matches_single_problem_calls(vf, vb):
     """Same bodies, same slabs and stages, same order: the batch reproduces the
     single-problem kernels of the same variant bit for bit."""
@@ -48,10 +48,9 @@ def test_batch_matches_single_problem_calls(vf, vb):
     b.run()
     torch.cuda.synchronize()
     assert not b.error()
-    # the single-problem kernels with the batch's bodies: forward 1, adjoint
-    # runs (6) or 2x2 blocks (4)
-    _lib.LIB.vp_set_kernel_variant(0, 1)
-    _lib.LIB.vp_set_kernel_variant(1, vb or 6)
+    # the single-problem kernels of the same variants
+    _lib.LIB.vp_set_kernel_variant(0, vf)
+    _lib.LIB.vp_set_kernel_variant(1, vb)
     try:
         for c, (yo, xo) in zip(cases, outs):
             SY, SX, H, n, PX = c["geom"]
@@ -73,14 +72,15 @@ def test_batch_matches_single_problem_calls(vf, vb):
 
 def test_batch_stages_on_large_problems():
     """Problems with several volume slabs (forward stages) and both angle
-    classes (adjoint stages) in one launch, against single-problem calls."""
+    classes (adjoint stages) in one launch, 8 heights per lane with a
+    half-filled second height chunk, against single-problem calls."""
     probs, refs = [], []
     for side, n in [(320, 60), (200, 45), (96, 30)]:
         a = torch.linspace(0, np.pi, n + 1, device="cuda")[:-1].contiguous()
-        x = torch.randn(side, side, 132, device="cuda")
-        y = torch.randn(n, side, 132, device="cuda")
-        yo = torch.zeros(n, side, 132, device="cuda")
-        xo = torch.zeros(side, side, 132, device="cuda")
+        x = torch.randn(side, side, 260, device="cuda")
+        y = torch.randn(n, side, 260, device="cuda")
+        yo = torch.zeros(n, side, 260, device="cuda")
+        xo = torch.zeros(side, side, 260, device="cuda")
         probs += [("forward", x, yo, a), ("backward", y, xo, a)]
         refs.append((x, y, yo, xo, a))
     b = Batch(probs)
@@ -88,9 +88,7 @@ def test_batch_stages_on_large_problems():
     b.run()  # runs accumulate: every output is now twice the operator
     torch.cuda.synchronize()
     assert not b.error()
-    _lib.LIB.vp_set_kernel_variant(0, 1)  # the single-problem kernels with the batch's bodies
-    _lib.LIB.vp_set_kernel_variant(1, 6)
-    try:
+    try:  # default variants on both sides
         for x, y, yo, xo, a in refs:
             ys = torch.zeros_like(yo)
             xs = torch.zeros_like(xo)
@@ -123,6 +121,24 @@ def test_batch_graph_replays_accumulate():
     torch.cuda.synchronize()
     assert rel_err(yo.cpu().numpy(), 3 * once.cpu().numpy()) < 1e-6
     assert rel_err(once.cpu().numpy(), oracle.forward(c["x"], c["ang"], 36, 0)) <= tol.REF_VS_FP64
+    b.close()
+
+
+def test_batch_launches_one_kernel_per_body():
+    """Problems of both directions and both height forms: one persistent
+    launch per body, four in all for any number of problems."""
+    probs = []
+    for side, H in [(40, 64), (36, 260), (48, 96), (30, 264)]:
+        a = torch.linspace(0, np.pi, 20, device="cuda")
+        x = torch.randn(side, side, H, device="cuda")
+        y = torch.randn(20, side, H, device="cuda")
+        probs += [("forward", x, torch.zeros_like(y), a), ("backward", y, torch.zeros_like(x), a)]
+    b = Batch(probs)
+    before = _lib.LIB.vp_launch_count()
+    b.run()
+    torch.cuda.synchronize()
+    assert _lib.LIB.vp_launch_count() - before == 4
+    assert not b.error()
     b.close()
 
 

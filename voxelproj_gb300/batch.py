@@ -1,21 +1,25 @@
-"""Batched projections in one persistent launch, replayable as a CUDA graph.
+"""Batched projections in persistent launches, replayable as a CUDA graph.
 
     b = Batch([("forward", x1, y1, angles1), ("backward", y2, x2, angles2, 4), ...])
-    b.run()                 # one persistent kernel launch for all problems
-    g = b.graph()           # CUDA graph of the same launch
+    b.run()                 # one persistent launch per body present (at most 4)
+    g = b.graph()           # CUDA graph of the same launches
     g.replay()
 
 Each problem is (op, in, out, angles[, variant]): op "forward" adds A in to
 out, "backward" adds A^T in to out.  The tensors are CUDA float32 in z_order 0
 layout (x (SY, SX, H), y (n_ang, PX, H)) with H a multiple of 4; the batch
-keeps references to them.  Variants (None: chosen by the autotuner for cube
-problems, library default otherwise) select each problem's work-item body.
+keeps references to them.  Variants are single-problem kernel variants
+(None: the library default; the benchmark below asks the autotuner) and
+select each problem's work-item body, heights per lane and volume slabs, so
+a batched problem's result equals the single-problem call of that variant.
+A body is the forward or the run adjoint with 4 or 8 heights per lane; each
+body present runs as one persistent kernel over all its problems' work items.
 
     python -m voxelproj_gb300.batch
 
 runs the uneven-batch workload: 64 cubes with sides drawn from
 {64, 96, ..., 384} and U{90..720} angles each, A for every cube and A^T for
-every sinogram, in one persistent launch replayed as a CUDA graph, next to
+every sinogram, in persistent launches replayed as a CUDA graph, next to
 the same work issued as sequential single-problem calls.  It prints one JSON
 line.
 """
@@ -77,8 +81,8 @@ class Batch:
         self.work_items = int(_lib.LIB.vp_batch_work_items(self._plan))
 
     def run(self, stream=None):
-        """Enqueue the whole batch (one persistent launch) on `stream`
-        (default: the current stream)."""
+        """Enqueue the whole batch (one persistent launch per body present)
+        on `stream` (default: the current stream)."""
         s = stream if stream is not None else torch.cuda.current_stream(self.device)
         with torch.cuda.device(self.device):
             _lib.check(_lib.LIB.vp_batch_run(self._plan, s.cuda_stream), "batch_run")
@@ -145,7 +149,9 @@ def main() -> None:
         plain.append((x, y_out, y, x_out, ang))
         vu += 2 * side**3 * n
     batch = Batch(problems)
+    before = _lib.LIB.vp_launch_count()
     graph = batch.graph()
+    launches = _lib.LIB.vp_launch_count() - before
 
     def timed(fn):
         fn()
@@ -166,6 +172,9 @@ def main() -> None:
             _CU.backward_z0(y, x_out, ang)
 
     t_seq = timed(sequential)
+    before = _lib.LIB.vp_launch_count()
+    sequential()
+    seq_launches = _lib.LIB.vp_launch_count() - before
     print(json.dumps({
         "workload": f"{args.count} cubes, sides {{64..384 step 32}}, U{{90..720}} angles each; "
                     "A of every cube and A^T of every sinogram",
@@ -173,7 +182,7 @@ def main() -> None:
         "graph_ms": round(t_graph, 3), "graph_gvu_s": round(vu / t_graph / 1e6, 1),
         "sequential_ms": round(t_seq, 3), "sequential_gvu_s": round(vu / t_seq / 1e6, 1),
         "speedup_vs_sequential": round(t_seq / t_graph, 3),
-        "launches_per_batch": 1,
+        "launches_per_batch": int(launches), "sequential_launches": int(seq_launches),
     }))
     batch.close()
 

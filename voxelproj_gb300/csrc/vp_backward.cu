@@ -300,6 +300,25 @@ cudaError_t launch_bp_z0_runs(const float* y, float* x, const float* angles, con
   return cudaSuccess;
 }
 
+// Runs with 8 heights per lane on heights [0, r8_heights(H)) and 4 on the
+// rest (one part when H <= 128 or the split leaves no remainder).
+int bp0_split(const Geom& g) { return g.H > 128 ? r8_heights(g.H) : 0; }
+
+cudaError_t launch_bp_z0_runs_split(const float* y, float* x, const float* angles,
+                                    const Geom& g, int row_lo, int row_hi,
+                                    cudaStream_t stream) {
+  const int H8 = bp0_split(g);
+  if (H8 > 0) {
+    Geom g8 = g;
+    g8.H = H8;
+    const cudaError_t e = launch_bp_z0_runs<8>(y, x, angles, g8, row_lo, row_hi, stream);
+    if (e != cudaSuccess || H8 == g.H) return e;
+  }
+  Geom g4 = g;
+  g4.H = g.H - H8;
+  return launch_bp_z0_runs<4>(y + H8, x + H8, angles, g4, row_lo, row_hi, stream);
+}
+
 bool bp0_vec4(const float* y, const float* x, const Geom& g) {
   return (g.Hx % 4 == 0) && (g.Hy % 4 == 0) &&
          ((reinterpret_cast<uintptr_t>(x) | reinterpret_cast<uintptr_t>(y)) & 15) == 0;
@@ -307,7 +326,9 @@ bool bp0_vec4(const float* y, const float* x, const Geom& g) {
 
 int launches_backward_z0(const float* y, const float* x, const Geom& g) {
   const int v = kernel_variant(OP_BACKWARD_Z0);
-  return (bp0_vec4(y, x, g) && (v < 1 || v > 5)) ? 2 : 1;  // runs: two launches
+  if (!bp0_vec4(y, x, g) || (v >= 1 && v <= 5)) return 1;
+  const int H8 = bp0_split(g);  // runs: two launches per height part
+  return (v != 6 && H8 > 0 && H8 < g.H) ? 4 : 2;
 }
 
 // Variants: 1 = one voxel run per warp (bp_z0_kernel); 2 = 4x4 register
@@ -315,8 +336,9 @@ int launches_backward_z0(const float* y, const float* x, const Geom& g) {
 // results equal the reference's bit for bit); 5 = 8x2; 6 = runs along the
 // axis of smaller step, two launches (bp_z0_runs_kernel); 7 = runs with 8
 // heights per lane (two float4, 128 heights apart; problems of at most 128
-// heights run 6).  The default when heights come in float4 is 7, the
-// fastest at 512^3 with 192 angles.
+// heights run 6, and a last chunk of at most 128 heights runs with 4 per
+// lane).  The default when heights come in float4 is 7, the fastest at 512^3
+// with 192 angles.
 cudaError_t launch_backward_z0(const float* y, float* x, const float* angles, const Geom& g,
                                cudaStream_t stream) {
   const bool vec4 = bp0_vec4(y, x, g);
@@ -328,9 +350,7 @@ cudaError_t launch_backward_z0(const float* y, float* x, const float* angles, co
       case 4: return launch_bp_z0_block<2, 2>(y, x, angles, g, stream);
       case 5: return launch_bp_z0_block<8, 2>(y, x, angles, g, stream);
       case 6: return launch_bp_z0_runs<4>(y, x, angles, g, 0, g.SY, stream);
-      default:
-        if (g.H > 128) return launch_bp_z0_runs<8>(y, x, angles, g, 0, g.SY, stream);
-        return launch_bp_z0_runs<4>(y, x, angles, g, 0, g.SY, stream);
+      default: return launch_bp_z0_runs_split(y, x, angles, g, 0, g.SY, stream);
     }
   }
   const int R = vec4 ? 4 : 1;
@@ -353,9 +373,9 @@ cudaError_t launch_backward_z0_rows(const float* y, float* x, const float* angle
                                     cudaStream_t stream) {
   if (row_lo == 0 && row_hi == g.SY) return launch_backward_z0(y, x, angles, g, stream);
   if (backward_z0_row_step(y, x, g) == 0 || row_lo % RUN != 0) return cudaErrorInvalidValue;
-  const int v = kernel_variant(OP_BACKWARD_Z0);
-  if (v != 6 && g.H > 128) return launch_bp_z0_runs<8>(y, x, angles, g, row_lo, row_hi, stream);
-  return launch_bp_z0_runs<4>(y, x, angles, g, row_lo, row_hi, stream);
+  if (kernel_variant(OP_BACKWARD_Z0) == 6)
+    return launch_bp_z0_runs<4>(y, x, angles, g, row_lo, row_hi, stream);
+  return launch_bp_z0_runs_split(y, x, angles, g, row_lo, row_hi, stream);
 }
 
 cudaError_t launch_backward_z2(const float* y, float* x, const float* angles, const Geom& g,

@@ -1,20 +1,24 @@
 // Batched projections: many problems of different sizes and angle counts,
-// A and A^T mixed, in one persistent launch.
+// A and A^T mixed, in one persistent launch per body (at most four).
 //
 // vp_batch_create validates the problems, splits each into work items and
 // uploads a descriptor table (the only allocations: the table, the stage
-// counters and an error flag).  vp_batch_run resets the counters and launches
-// one persistent kernel with a full wave of blocks (SMs x resident blocks).
+// counters and an error flag).  vp_batch_run resets the counters and, for
+// each body present (forward or run adjoint, 4 or 8 heights per lane),
+// launches one persistent kernel with a full wave of blocks (SMs x resident
+// blocks).
 // Each block repeatedly takes the next item from a global counter, finds its
-// problem by binary search and runs the same per-warp bodies as the
-// single-problem kernels:
-//   forward item = (problem, 128-height chunk, volume slab, angle, 4 bin runs)
-//   adjoint item = (problem, 128-height chunk, angle class, 4 voxel runs)
+// problem by binary search and runs the same per-warp bodies, with the same
+// heights per lane and the same volume slabs, as the single-problem kernel
+// of the problem's variant:
+//   forward item = (problem, height chunk, volume slab, angle, 4 bin runs)
+//   adjoint item = (problem, height chunk, angle class, 4 voxel runs)
 //                  or, variant 4, (problem, chunk, 4 voxel blocks of 2x2)
-// Items are numbered problem by problem, heights slowest, so blocks running
-// together share one problem and height chunk and its working set stays in
-// L2 (as the single-problem kernels' slabs and height ordering do); the
-// dynamic counter balances problems of very different sizes.
+// A height chunk is 32 lanes x 4 or 8 heights.  Items are numbered problem
+// by problem, heights slowest, so blocks running together share one problem
+// and height chunk and its working set stays in L2 (as the single-problem
+// kernels' slabs and height ordering do); the dynamic counter balances
+// problems of very different sizes.
 //
 // Stages.  The forward's volume slabs all add into the same sinogram bins,
 // and the run adjoint's two angle classes into the same voxels.  Within a
@@ -61,12 +65,14 @@ struct BatchDesc {
   const float* angles;
   Geom g;
   long long begin;      // first global item of this problem
-  long long per_chunk;  // items per 128-height chunk
+  long long per_chunk;  // items per height chunk
   int kind;
+  int R;                // heights per lane: 4, or 8 as two float4 128 apart
   int nstages;          // stages per chunk
   int counter_base;     // first stage counter of this problem
-  // forward: slab rows, bin groups per angle
-  int slab_rows, units;
+  // forward: slab plan (class slabs, rows and columns per slab), bin groups
+  // per angle
+  int cls, wy, wx, units;
   // run adjoint: runs and run groups of each class
   int nruns0, groups0, nruns1, groups1;
   // block adjoint: blocks along x, blocks, block groups
@@ -115,50 +121,69 @@ __device__ __forceinline__ void signal_done(unsigned* counter) {
   }
 }
 
-__device__ __forceinline__ void run_fwd_item(const BatchDesc& d, long long local, int stage,
-                                             long long in_stage, int hc, BatchSmem& sm, int w,
-                                             int lane, unsigned* counters, int* error) {
-  const int a = (int)(in_stage / d.units);
-  const int bg = (int)(in_stage % d.units);
-  const int y_lo = stage * d.slab_rows;
-  const int y_hi = min(d.g.SY, y_lo + d.slab_rows);
+template <int R>
+__device__ __forceinline__ void run_fwd_item(const BatchDesc& d, int stage, int in_stage,
+                                             int hc, BatchSmem& sm, int w, int lane,
+                                             unsigned* counters, int* error) {
+  constexpr int UN = R == 8 ? 2 : FP0_UNROLL;  // as the single-problem kernels
+  const int a = in_stage / d.units;
+  const int bg = in_stage - a * d.units;
+  const Slab slab = slab_of(stage, d.cls, d.wy, d.wx, d.g.SY, d.g.SX);
   unsigned* ctr = counters + d.counter_base + hc * d.nstages + stage;
   const int p0 = (bg * BATCH_WARPS + w) * 4;
-  const int h = (hc * 32 + lane) * 4;
+  const int h = hc * 32 * R + lane * 4;
   if (stage == 0) {
-    fp_z0_warp<4, 4>(d.in, d.out, d.angles, d.g, p0, a, h, row_slab(y_lo, y_hi, d.g.SX), 1,
-                     sm.cand[w]);
+    fp_z0_warp<R, 4, UN>(d.in, d.out, d.angles, d.g, p0, a, h, slab, 1, sm.cand[w]);
   } else {
     const StageWait wt{ctr - 1, (unsigned)(d.g.n_ang * d.units * BATCH_WARPS), error};
-    fp_z0_warp<4, 4>(d.in, d.out, d.angles, d.g, p0, a, h, row_slab(y_lo, y_hi, d.g.SX), 1,
-                     sm.cand[w], wt);
+    fp_z0_warp<R, 4, UN>(d.in, d.out, d.angles, d.g, p0, a, h, slab, 1, sm.cand[w], wt);
   }
   signal_done(ctr);
 }
 
-__device__ __forceinline__ void run_bwd_runs_item(const BatchDesc& d, int stage, long long grp,
+template <int R>
+__device__ __forceinline__ void run_bwd_runs_item(const BatchDesc& d, int stage, int grp,
                                                   int hc, BatchSmem& sm, int w, int lane,
                                                   unsigned* counters, int* error) {
   unsigned* ctr = counters + d.counter_base + hc * d.nstages + stage;
-  const int run = (int)grp * BATCH_WARPS + w;
-  const int h = (hc * 32 + lane) * 4;
+  const int run = grp * BATCH_WARPS + w;
+  const int h = hc * 32 * R + lane * 4;
   if (stage == 0) {
     if (run < d.nruns0) {
       const int nmaj = (d.g.SX + RUN - 1) / RUN;
-      bp_runs_warp<0>(d.in, d.out, d.angles, d.g, (run % nmaj) * RUN, run / nmaj, h, 1,
-                      sm.runs.tab[w], sm.runs.alist[w]);
+      bp_runs_warp<0, R>(d.in, d.out, d.angles, d.g, (run % nmaj) * RUN, run / nmaj, h, 1,
+                         sm.runs.tab[w], sm.runs.alist[w]);
     }
   } else if (run < d.nruns1) {
     const StageWait wt{ctr - 1, (unsigned)(d.groups0 * BATCH_WARPS), error};
-    bp_runs_warp<1>(d.in, d.out, d.angles, d.g, run % d.g.SX, (run / d.g.SX) * RUN, h, 1,
-                    sm.runs.tab[w], sm.runs.alist[w], wt);
+    bp_runs_warp<1, R>(d.in, d.out, d.angles, d.g, run % d.g.SX, (run / d.g.SX) * RUN, h, 1,
+                       sm.runs.tab[w], sm.runs.alist[w], wt);
   }
   signal_done(ctr);
 }
 
-// 7 resident blocks per SM (72 registers), the occupancy of the
-// single-problem run adjoint; the few spilled values are item bookkeeping.
-__global__ void __launch_bounds__(BATCH_THREADS, 7)
+// One kernel instance per body: the forward or the run adjoint with 4 or 8
+// heights per lane (the 2x2 block adjoint rides with the 4-height adjoint).
+// Each instance gets the register allocation of its single-problem kernel, so
+// no body runs at another body's occupancy; a plan launches the instances of
+// the bodies it holds, one persistent launch each.
+constexpr int B_FWD4 = 0, B_FWD8 = 1, B_BWD4 = 2, B_BWD8 = 3, NBODIES = 4;
+
+__host__ __device__ inline int body_of(const BatchDesc& d) {
+  if (d.kind == K_FWD) return d.R == 8 ? B_FWD8 : B_FWD4;
+  return (d.kind == K_BWD_RUNS && d.R == 8) ? B_BWD8 : B_BWD4;
+}
+
+// Resident blocks per SM the registers must allow, so that each body keeps
+// about its single-problem kernel's occupancy despite the item bookkeeping:
+// 8-height forward 6 (79 registers), 4-height forward 7 (72), 8-height run
+// adjoint 5 (96); the 4-height adjoints as the compiler chooses (72).
+constexpr int batch_min_blocks(int body) {
+  return body == B_FWD8 ? 6 : body == B_FWD4 ? 7 : body == B_BWD8 ? 5 : 0;
+}
+
+template <int BODY>
+__global__ void __launch_bounds__(BATCH_THREADS, batch_min_blocks(BODY))
     batch_kernel(const BatchDesc* __restrict__ descs, int ndesc, long long total,
                  unsigned long long* __restrict__ next, unsigned* __restrict__ counters,
                  int* __restrict__ error) {
@@ -177,19 +202,23 @@ __global__ void __launch_bounds__(BATCH_THREADS, 7)
       if (descs[mid].begin <= item) lo = mid; else hi = mid - 1;
     }
     const BatchDesc d = descs[lo];
-    const long long local = item - d.begin;
-    const int hc = (int)(local / d.per_chunk);
-    const long long in_chunk = local % d.per_chunk;
-    if (d.kind == K_FWD) {
-      const long long per_stage = (long long)d.g.n_ang * d.units;
-      run_fwd_item(d, local, (int)(in_chunk / per_stage), in_chunk % per_stage, hc, sm, w, lane,
-                   counters, error);
-    } else if (d.kind == K_BWD_RUNS) {
+    // 32-bit index arithmetic: a problem's items fit in an int (checked when
+    // the plan is made)
+    const int local = (int)(item - d.begin);
+    const int hc = local / (int)d.per_chunk;
+    const int in_chunk = local - hc * (int)d.per_chunk;
+    if constexpr (BODY == B_FWD4 || BODY == B_FWD8) {
+      constexpr int R = BODY == B_FWD8 ? 8 : 4;
+      const int per_stage = d.g.n_ang * d.units;
+      const int stage = in_chunk / per_stage;
+      run_fwd_item<R>(d, stage, in_chunk - stage * per_stage, hc, sm, w, lane, counters, error);
+    } else if (BODY == B_BWD8 || d.kind == K_BWD_RUNS) {
+      constexpr int R = BODY == B_BWD8 ? 8 : 4;
       const bool first = in_chunk < d.groups0;
-      run_bwd_runs_item(d, first ? 0 : 1, first ? in_chunk : in_chunk - d.groups0, hc, sm, w,
-                        lane, counters, error);
+      run_bwd_runs_item<R>(d, first ? 0 : 1, first ? in_chunk : in_chunk - d.groups0, hc, sm,
+                           w, lane, counters, error);
     } else {
-      const int bidx = (int)in_chunk * BATCH_WARPS + w;
+      const int bidx = in_chunk * BATCH_WARPS + w;
       if (bidx < d.nblocks)
         bp_block_warp<2, 2>(d.in, d.out, d.angles, d.g, (bidx % d.nbx) * 2, (bidx / d.nbx) * 2,
                             (hc * 32 + lane) * 4, 1,
@@ -201,24 +230,88 @@ __global__ void __launch_bounds__(BATCH_THREADS, 7)
 
 unsigned ceil_div_u(long long a, long long b) { return (unsigned)((a + b - 1) / b); }
 
+using BatchKernelFn = void (*)(const BatchDesc*, int, long long, unsigned long long*, unsigned*,
+                               int*);
+
+const void* batch_kernel_for(int body) {
+  static const BatchKernelFn fns[NBODIES] = {batch_kernel<B_FWD4>, batch_kernel<B_FWD8>,
+                                             batch_kernel<B_BWD4>, batch_kernel<B_BWD8>};
+  return reinterpret_cast<const void*>(fns[body]);
+}
+
 }  // namespace
 }  // namespace vp
 
 struct vp_batch_plan {
   int device = 0;
-  vp::BatchDesc* d_descs = nullptr;
-  unsigned long long* d_next = nullptr;
+  vp::BatchDesc* d_descs = nullptr;     // grouped by body, problem order within a body
+  unsigned long long* d_next = nullptr;  // one item counter per body
   unsigned* d_counters = nullptr;
   int* d_error = nullptr;
-  int ndesc = 0;
   int ncounters = 0;
   long long total = 0;
-  int grid = 0;
+  // per body: first descriptor, descriptors, items, grid (0: body absent)
+  int first[vp::NBODIES] = {};
+  int ndesc[vp::NBODIES] = {};
+  long long items[vp::NBODIES] = {};
+  int grid[vp::NBODIES] = {};
 };
 
 namespace {
 
-int batch_desc(const vp_batch_problem& p, vp::BatchDesc* d, bool* empty) {
+// Work items of one height part: heights [0, g.H) of in / out, R heights
+// per lane for the runs adjoint (the forward takes R from its plan).
+int part_desc(const vp_batch_problem& p, const vp::Geom& g, const float* in, float* out, int R,
+              vp::BatchDesc* d) {
+  std::memset(d, 0, sizeof(*d));
+  d->g = g;
+  d->in = in;
+  d->out = out;
+  d->angles = p.angles;
+  if (p.op == VP_OP_FORWARD) {
+    // the single-problem forward's plan for this variant (0: its default)
+    const vp::Fp0Plan pl = vp::forward_z0_plan(g, true, p.variant);
+    if (pl.KW != 4 || pl.agroup || (pl.R == 8 ? pl.un != 2 : pl.un != vp::detail::FP0_UNROLL))
+      return VP_ERR_BATCH;  // bodies the batch does not carry
+    d->kind = vp::K_FWD;
+    d->R = pl.R;
+    d->cls = pl.cls ? 1 : 0;
+    d->wy = pl.wy;
+    d->wx = pl.wx;
+    d->nstages = pl.nslabs;
+    d->units = (int)vp::ceil_div_u(g.PX, 4ll * vp::BATCH_WARPS);
+    d->per_chunk = (long long)d->nstages * g.n_ang * d->units;
+  } else if (p.variant == 0 || p.variant == 6 || p.variant == 7) {
+    d->kind = vp::K_BWD_RUNS;
+    d->R = R;
+    d->nstages = 2;
+    d->nruns0 = (int)vp::ceil_div_u(g.SX, vp::detail::RUN) * g.SY;
+    d->nruns1 = g.SX * (int)vp::ceil_div_u(g.SY, vp::detail::RUN);
+    d->groups0 = (int)vp::ceil_div_u(d->nruns0, vp::BATCH_WARPS);
+    d->groups1 = (int)vp::ceil_div_u(d->nruns1, vp::BATCH_WARPS);
+    d->per_chunk = (long long)d->groups0 + d->groups1;
+  } else if (p.variant == 4) {
+    d->kind = vp::K_BWD_BLOCK;
+    d->R = 4;
+    d->nstages = 1;
+    d->nbx = (int)vp::ceil_div_u(g.SX, 2);
+    d->nblocks = d->nbx * (int)vp::ceil_div_u(g.SY, 2);
+    d->bgroups = (int)vp::ceil_div_u(d->nblocks, vp::BATCH_WARPS);
+    d->per_chunk = d->bgroups;
+  } else {
+    return VP_ERR_BATCH;
+  }
+  const long long hch = (g.H + 32 * d->R - 1) / (32 * d->R);
+  if (hch * d->per_chunk >= (1ll << 31)) return VP_ERR_BATCH;  // items indexed as int
+  d->begin = hch * d->per_chunk;              // item count, turned into offsets later
+  d->counter_base = (int)(hch * d->nstages);  // counter count, turned into offsets later
+  return VP_OK;
+}
+
+// The problem's descriptors: one per height part.  With 8 heights per lane a
+// last chunk of at most 128 heights is a second part with 4 per lane, as in
+// the single-problem launchers (r8_heights).
+int batch_desc(const vp_batch_problem& p, std::vector<vp::BatchDesc>* out) {
   if (p.op != VP_OP_FORWARD && p.op != VP_OP_BACKWARD) return VP_ERR_BATCH;
   if (p.flags & ~VP_FLAG_TRIG_PRECISE) return VP_ERR_BAD_FLAGS;
   const bool fwd = p.op == VP_OP_FORWARD;
@@ -229,14 +322,13 @@ int batch_desc(const vp_batch_problem& p, vp::BatchDesc* d, bool* empty) {
   if (xd[0] * xd[1] >= ((int64_t)1 << 27)) return VP_ERR_BAD_SHAPE;
   if (yd[0] > 0 && p.n_angles < yd[0]) return VP_ERR_ANGLES;
   const int64_t H = xd[2] < yd[2] ? xd[2] : yd[2];
-  *empty = xd[0] == 0 || xd[1] == 0 || yd[0] == 0 || yd[1] == 0 || H == 0;
-  if (*empty) return VP_OK;
+  if (xd[0] == 0 || xd[1] == 0 || yd[0] == 0 || yd[1] == 0 || H == 0) return VP_OK;  // empty
   if (!p.in || !p.out || !p.angles) return VP_ERR_NULL_POINTER;
   // the batched bodies read and write heights as float4
   if ((xd[2] % 4) || (yd[2] % 4) ||
       ((reinterpret_cast<uintptr_t>(p.in) | reinterpret_cast<uintptr_t>(p.out)) & 15))
     return VP_ERR_BATCH;
-  vp::Geom& g = d->g;
+  vp::Geom g;
   g.SY = (int)xd[0];
   g.SX = (int)xd[1];
   g.Hx = (int)xd[2];
@@ -249,40 +341,24 @@ int batch_desc(const vp_batch_problem& p, vp::BatchDesc* d, bool* empty) {
   g.pcent = 0.5f * (float)(g.PX - 1);
   g.trig = (p.flags & VP_FLAG_TRIG_PRECISE) ? vp::TRIG_PRECISE : vp::TRIG_REF;
   g.accumulate = 1;
-  d->in = p.in;
-  d->out = p.out;
-  d->angles = p.angles;
-  const long long hch = (H + 127) / 128;
-  if (fwd) {
-    if (p.variant != 0 && p.variant != 1) return VP_ERR_BATCH;
-    d->kind = vp::K_FWD;
-    // about 32 MB of one 128-height chunk of the volume per slab
-    long long rows = (32ll << 20) / ((long long)g.SX * 128 * 4);
-    rows = rows < 8 ? 8 : rows;
-    d->slab_rows = (int)(rows < g.SY ? rows : g.SY);
-    d->nstages = (int)vp::ceil_div_u(g.SY, d->slab_rows);
-    d->units = (int)vp::ceil_div_u(g.PX, 4ll * vp::BATCH_WARPS);
-    d->per_chunk = (long long)d->nstages * g.n_ang * d->units;
-  } else if (p.variant == 0 || p.variant == 6) {
-    d->kind = vp::K_BWD_RUNS;
-    d->nstages = 2;
-    d->nruns0 = (int)vp::ceil_div_u(g.SX, vp::detail::RUN) * g.SY;
-    d->nruns1 = g.SX * (int)vp::ceil_div_u(g.SY, vp::detail::RUN);
-    d->groups0 = (int)vp::ceil_div_u(d->nruns0, vp::BATCH_WARPS);
-    d->groups1 = (int)vp::ceil_div_u(d->nruns1, vp::BATCH_WARPS);
-    d->per_chunk = (long long)d->groups0 + d->groups1;
-  } else if (p.variant == 4) {
-    d->kind = vp::K_BWD_BLOCK;
-    d->nstages = 1;
-    d->nbx = (int)vp::ceil_div_u(g.SX, 2);
-    d->nblocks = d->nbx * (int)vp::ceil_div_u(g.SY, 2);
-    d->bgroups = (int)vp::ceil_div_u(d->nblocks, vp::BATCH_WARPS);
-    d->per_chunk = d->bgroups;
-  } else {
-    return VP_ERR_BATCH;
+  // heights per lane of the first part
+  int R = 4;
+  if (fwd)
+    R = vp::forward_z0_plan(g, true, p.variant).R;
+  else if ((p.variant == 0 || p.variant == 7) && H > 128)
+    R = 8;
+  const int H8 = R == 8 ? vp::r8_heights(g.H) : g.H;
+  vp::BatchDesc d;
+  vp::Geom g0 = g;
+  g0.H = H8;
+  if (int st = part_desc(p, g0, p.in, p.out, R, &d)) return st;
+  out->push_back(d);
+  if (H8 < g.H) {
+    vp::Geom g1 = g;
+    g1.H = g.H - H8;
+    if (int st = part_desc(p, g1, p.in + H8, p.out + H8, 4, &d)) return st;
+    out->push_back(d);
   }
-  d->begin = hch * d->per_chunk;  // item count, turned into offsets later
-  d->counter_base = (int)(hch * d->nstages);  // counter count, turned into offsets later
   return VP_OK;
 }
 
@@ -295,35 +371,52 @@ int vp_batch_create(const vp_batch_problem* problems, int count, vp_batch_plan**
   if (count < 0) return VP_ERR_BATCH;
   *plan = nullptr;
   std::vector<vp::BatchDesc> descs;
-  descs.reserve(count);
-  long long total = 0;
-  long long ncounters = 0;
+  descs.reserve(2 * (size_t)count);
+  // descriptors grouped by body; items numbered from 0 within each body
+  std::vector<vp::BatchDesc> by_body[vp::NBODIES];
+  std::vector<vp::BatchDesc> parts;
   for (int i = 0; i < count; ++i) {
-    vp::BatchDesc d;
-    std::memset(&d, 0, sizeof(d));
-    bool empty = false;
-    if (int s = batch_desc(problems[i], &d, &empty)) return s;
-    if (empty) continue;
-    const long long n = d.begin;
-    d.begin = total;
-    total += n;
-    const long long nc = d.counter_base;
-    d.counter_base = (int)ncounters;
-    ncounters += nc;
-    descs.push_back(d);
+    parts.clear();
+    if (int s = batch_desc(problems[i], &parts)) return s;
+    for (const vp::BatchDesc& d : parts) by_body[vp::body_of(d)].push_back(d);
   }
-  if (ncounters >= (1ll << 31)) return VP_ERR_BATCH;
   vp_batch_plan* pl = new (std::nothrow) vp_batch_plan;
   if (pl == nullptr) return VP_ERR_BATCH;
+  long long ncounters = 0;
+  for (int b = 0; b < vp::NBODIES; ++b) {
+    pl->first[b] = (int)descs.size();
+    long long items = 0;
+    for (vp::BatchDesc d : by_body[b]) {
+      const long long n = d.begin;
+      d.begin = items;
+      items += n;
+      const long long nc = d.counter_base;
+      d.counter_base = (int)ncounters;
+      ncounters += nc;
+      descs.push_back(d);
+    }
+    pl->ndesc[b] = (int)by_body[b].size();
+    pl->items[b] = items;
+    pl->total += items;
+  }
+  if (ncounters >= (1ll << 31)) {
+    delete pl;
+    return VP_ERR_BATCH;
+  }
   cudaError_t e = cudaGetDevice(&pl->device);
-  int sms = 0, per_sm = 0;
+  int sms = 0;
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, pl->device);
-  if (e == cudaSuccess)
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, vp::batch_kernel,
+  for (int b = 0; b < vp::NBODIES && e == cudaSuccess; ++b) {
+    if (pl->items[b] == 0) continue;
+    int per_sm = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, vp::batch_kernel_for(b),
                                                       vp::BATCH_THREADS, 0);
+    const long long wave = (long long)sms * (per_sm > 0 ? per_sm : 1);
+    pl->grid[b] = (int)(pl->items[b] < wave ? pl->items[b] : wave);
+  }
   if (e == cudaSuccess && !descs.empty())
     e = cudaMalloc(&pl->d_descs, descs.size() * sizeof(vp::BatchDesc));
-  if (e == cudaSuccess) e = cudaMalloc(&pl->d_next, sizeof(unsigned long long));
+  if (e == cudaSuccess) e = cudaMalloc(&pl->d_next, vp::NBODIES * sizeof(unsigned long long));
   if (e == cudaSuccess && ncounters > 0) e = cudaMalloc(&pl->d_counters, ncounters * sizeof(unsigned));
   if (e == cudaSuccess) e = cudaMalloc(&pl->d_error, sizeof(int));
   if (e == cudaSuccess && !descs.empty())
@@ -334,11 +427,7 @@ int vp_batch_create(const vp_batch_problem* problems, int count, vp_batch_plan**
     vp_batch_destroy(pl);
     return vp::record_cuda_error(e);
   }
-  pl->ndesc = (int)descs.size();
   pl->ncounters = (int)ncounters;
-  pl->total = total;
-  const long long wave = (long long)sms * (per_sm > 0 ? per_sm : 1);
-  pl->grid = (int)(total < wave ? total : wave);
   *plan = pl;
   return VP_OK;
 }
@@ -347,15 +436,21 @@ int vp_batch_run(vp_batch_plan* plan, void* stream) {
   if (plan == nullptr) return VP_ERR_NULL_POINTER;
   if (plan->total == 0) return VP_OK;
   cudaStream_t st = (cudaStream_t)stream;
-  cudaError_t e = cudaMemsetAsync(plan->d_next, 0, sizeof(unsigned long long), st);
+  cudaError_t e = cudaMemsetAsync(plan->d_next, 0, vp::NBODIES * sizeof(unsigned long long), st);
   if (e == cudaSuccess && plan->ncounters > 0)
     e = cudaMemsetAsync(plan->d_counters, 0, (size_t)plan->ncounters * sizeof(unsigned), st);
-  if (e == cudaSuccess) {
-    vp::batch_kernel<<<plan->grid, vp::BATCH_THREADS, 0, st>>>(
-        plan->d_descs, plan->ndesc, plan->total, plan->d_next, plan->d_counters, plan->d_error);
-    e = cudaGetLastError();
+  int launched = 0;
+  for (int b = 0; b < vp::NBODIES && e == cudaSuccess; ++b) {
+    if (plan->items[b] == 0) continue;
+    const vp::BatchDesc* descs = plan->d_descs + plan->first[b];
+    unsigned long long* next = plan->d_next + b;
+    void* args[] = {&descs, &plan->ndesc[b], &plan->items[b], &next, &plan->d_counters,
+                    &plan->d_error};
+    e = cudaLaunchKernel(vp::batch_kernel_for(b), dim3(plan->grid[b]), dim3(vp::BATCH_THREADS),
+                         args, 0, st);
+    ++launched;
   }
-  vp::count_launches(1);
+  vp::count_launches(launched);
   return e == cudaSuccess ? VP_OK : vp::record_cuda_error(e);
 }
 

@@ -183,18 +183,21 @@ int fp0_slabs(const Geom& g, const Fp0Config& c) {
   return (int)(n < 1 ? 1 : n);
 }
 
-Slab fp0_slab(const Geom& g, const Fp0Config& c, int k, int n) {
+// Rows (and, for class slabs, columns) per slab.
+void fp0_slab_widths(const Geom& g, const Fp0Config& c, int n, int* wy, int* wx) {
   if (!c.cls) {
-    const int rows = fp0_slab_rows(g, c);
-    const int y_lo = k * rows;
-    return row_slab(y_lo, y_lo + rows < g.SY ? y_lo + rows : g.SY, g.SX);
+    *wy = fp0_slab_rows(g, c);
+    *wx = g.SX;
+  } else {
+    *wy = (g.SY + n - 1) / n;
+    *wx = (g.SX + n - 1) / n;
   }
-  const int wy = (g.SY + n - 1) / n;
-  const int wx = (g.SX + n - 1) / n;
-  const int y_lo = k * wy < g.SY ? k * wy : g.SY;
-  const int x_lo = k * wx < g.SX ? k * wx : g.SX;
-  return Slab{y_lo, y_lo + wy < g.SY ? y_lo + wy : g.SY,
-              x_lo, x_lo + wx < g.SX ? x_lo + wx : g.SX, 0, g.SY};
+}
+
+Slab fp0_slab(const Geom& g, const Fp0Config& c, int k, int n) {
+  int wy = 0, wx = 0;
+  fp0_slab_widths(g, c, n, &wy, &wx);
+  return slab_of(k, c.cls, wy, wx, g.SY, g.SX);
 }
 
 bool fp0_vec4(const float* x, const float* y, const Geom& g) {
@@ -202,11 +205,7 @@ bool fp0_vec4(const float* x, const float* y, const Geom& g) {
          ((reinterpret_cast<uintptr_t>(x) | reinterpret_cast<uintptr_t>(y)) & 15) == 0;
 }
 
-int launches_forward_z0(const float* x, const float* y, const Geom& g) {
-  const Fp0Config c = fp0_config(g, fp0_vec4(x, y, g), kernel_variant(OP_FORWARD_Z0));
-  const long long per = c.agroup ? (long long)kMaxGridYZ * FP0_WARPS : kMaxGridYZ;
-  return (int)(fp0_slabs(g, c) * ceil_div(g.n_ang, per));
-}
+int launches_forward_z0(const float* x, const float* y, const Geom& g);
 
 int launches_forward_z2(const Geom& g) {
   return (int)ceil_div(g.n_ang, (long long)kMaxGridYZ * FP2_WARPS);
@@ -261,40 +260,119 @@ cudaError_t launch_fp_z0_config(const float* x, float* y, const float* angles, c
   return launch_fp_z0_r<1>(x, y, angles, g, c, k0, k1, stream);
 }
 
+// The heights of a call as (first height, count) parts: one part, or with 8
+// heights per lane an 8-height part and a 4-height remainder (r8_heights).
+struct HeightParts {
+  int n;
+  Geom g[2];
+  int h0[2];
+};
+
+HeightParts fp0_parts(const Geom& g, bool vec4, int variant) {
+  HeightParts p{1, {g, g}, {0, 0}};
+  if (fp0_config(g, vec4, variant).R == 8) {
+    const int H8 = r8_heights(g.H);
+    if (H8 < g.H) {
+      p.n = 2;
+      p.g[0].H = H8;
+      p.g[1].H = g.H - H8;
+      p.h0[1] = H8;
+    }
+  }
+  return p;
+}
+
 cudaError_t launch_forward_z0(const float* x, float* y, const float* angles, const Geom& g,
                               cudaStream_t stream) {
-  const Fp0Config c = fp0_config(g, fp0_vec4(x, y, g), kernel_variant(OP_FORWARD_Z0));
-  return launch_fp_z0_config(x, y, angles, g, c, 0, 1 << 30, stream);
+  const bool vec4 = fp0_vec4(x, y, g);
+  const int v = kernel_variant(OP_FORWARD_Z0);
+  const HeightParts hp = fp0_parts(g, vec4, v);
+  for (int i = 0; i < hp.n; ++i) {
+    const Fp0Config c = fp0_config(hp.g[i], vec4, v);
+    const cudaError_t e = launch_fp_z0_config(x + hp.h0[i], y + hp.h0[i], angles, hp.g[i], c, 0,
+                                              1 << 30, stream);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+Fp0Plan forward_z0_plan(const Geom& g, bool vec4, int variant) {
+  const Fp0Config c = fp0_config(g, vec4, variant);
+  Fp0Plan p;
+  p.R = c.R;
+  p.KW = c.KW;
+  p.un = c.un;
+  p.agroup = c.agroup;
+  p.cls = c.cls;
+  p.nslabs = fp0_slabs(g, c);
+  fp0_slab_widths(g, c, p.nslabs, &p.wy, &p.wx);
+  return p;
+}
+
+int launches_forward_z0(const float* x, const float* y, const Geom& g) {
+  const bool vec4 = fp0_vec4(x, y, g);
+  const int v = kernel_variant(OP_FORWARD_Z0);
+  const HeightParts hp = fp0_parts(g, vec4, v);
+  int n = 0;
+  for (int i = 0; i < hp.n; ++i) {
+    const Fp0Config c = fp0_config(hp.g[i], vec4, v);
+    const long long per = c.agroup ? (long long)kMaxGridYZ * FP0_WARPS : kMaxGridYZ;
+    n += (int)(fp0_slabs(hp.g[i], c) * ceil_div(hp.g[i].n_ang, per));
+  }
+  return n;
 }
 
 // Row-slab form of the selected variant, for volumes that arrive in row
-// order: slab k reads only rows [forward_z0_row_slab(k)).
-Fp0Config fp0_stream_config(const float* x, const float* y, const Geom& g) {
-  Fp0Config c = fp0_config(g, fp0_vec4(x, y, g), kernel_variant(OP_FORWARD_Z0));
+// order: slab k of the main height part reads only rows
+// [forward_z0_row_slab(k)); the 4-height remainder of a split (if any) runs
+// whole once every row is in (launch_forward_z0_row_rest).
+Fp0Config fp0_stream_config(const Geom& g, bool vec4) {
+  Fp0Config c = fp0_config(g, vec4, kernel_variant(OP_FORWARD_Z0));
   c.cls = false;
   return c;
 }
 
+Geom fp0_stream_main(const float* x, const float* y, const Geom& g) {
+  return fp0_parts(g, fp0_vec4(x, y, g), kernel_variant(OP_FORWARD_Z0)).g[0];
+}
+
 int forward_z0_row_slabs(const float* x, const float* y, const Geom& g) {
-  return fp0_slabs(g, fp0_stream_config(x, y, g));
+  const Geom gm = fp0_stream_main(x, y, g);
+  return fp0_slabs(gm, fp0_stream_config(gm, fp0_vec4(x, y, g)));
 }
 
 void forward_z0_row_slab(const float* x, const float* y, const Geom& g, int k, int* row_lo,
                          int* row_hi) {
-  const Fp0Config c = fp0_stream_config(x, y, g);
-  const Slab s = fp0_slab(g, c, k, fp0_slabs(g, c));
+  const Geom gm = fp0_stream_main(x, y, g);
+  const Fp0Config c = fp0_stream_config(gm, fp0_vec4(x, y, g));
+  const Slab s = fp0_slab(gm, c, k, fp0_slabs(gm, c));
   *row_lo = s.y_lo;
   *row_hi = s.y_hi;
 }
 
 cudaError_t launch_forward_z0_row_slab(const float* x, float* y, const float* angles,
                                        const Geom& g, int k, cudaStream_t stream) {
-  return launch_fp_z0_config(x, y, angles, g, fp0_stream_config(x, y, g), k, k + 1, stream);
+  const Geom gm = fp0_stream_main(x, y, g);
+  return launch_fp_z0_config(x, y, angles, gm, fp0_stream_config(gm, fp0_vec4(x, y, g)), k,
+                             k + 1, stream);
 }
 
 int forward_z0_row_slab_launches(const float* x, const float* y, const Geom& g) {
-  const Fp0Config c = fp0_stream_config(x, y, g);
+  const Geom gm = fp0_stream_main(x, y, g);
+  const Fp0Config c = fp0_stream_config(gm, fp0_vec4(x, y, g));
   return (int)ceil_div(g.n_ang, c.agroup ? (long long)kMaxGridYZ * FP0_WARPS : kMaxGridYZ);
+}
+
+cudaError_t launch_forward_z0_row_rest(const float* x, float* y, const float* angles,
+                                       const Geom& g, cudaStream_t stream, int* launches) {
+  const bool vec4 = fp0_vec4(x, y, g);
+  const HeightParts hp = fp0_parts(g, vec4, kernel_variant(OP_FORWARD_Z0));
+  if (hp.n < 2) return cudaSuccess;
+  const Fp0Config c = fp0_stream_config(hp.g[1], vec4);
+  *launches += fp0_slabs(hp.g[1], c) *
+               (int)ceil_div(g.n_ang, c.agroup ? (long long)kMaxGridYZ * FP0_WARPS : kMaxGridYZ);
+  return launch_fp_z0_config(x + hp.h0[1], y + hp.h0[1], angles, hp.g[1], c, 0, 1 << 30,
+                             stream);
 }
 
 cudaError_t launch_forward_z2(const float* x, float* y, const float* angles, const Geom& g,

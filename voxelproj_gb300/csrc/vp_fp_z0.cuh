@@ -104,6 +104,17 @@ __host__ __device__ inline Slab row_slab(int y_lo, int y_hi, int SX) {
   return Slab{y_lo, y_hi, 0, SX, y_lo, y_hi};
 }
 
+// Slab k of a slab plan: row slabs of wy rows, or class slabs of wy rows and
+// wx columns (ranges clamped to the volume).
+__host__ __device__ inline Slab slab_of(int k, bool cls, int wy, int wx, int SY, int SX) {
+  const int y_lo = k * wy < SY ? k * wy : SY;
+  const int y_hi = y_lo + wy < SY ? y_lo + wy : SY;
+  if (!cls) return row_slab(y_lo, y_hi, SX);
+  const int x_lo = k * wx < SX ? k * wx : SX;
+  const int x_hi = x_lo + wx < SX ? x_lo + wx : SX;
+  return Slab{y_lo, y_hi, x_lo, x_hi, 0, SY};
+}
+
 // One warp: angle a, bins [p0, p0 + KW), this lane's heights from h (LaneH:
 // R = 8 is [h, h + 4) and [h + 128, h + 132)), the voxels of slab s.
 // UN candidates are loaded together.  cand is this warp's shared candidate list of

@@ -4,7 +4,8 @@
 // Forward, y_host (+)= A x_host:
 //   copy stream:  angles, x rows of slab 0, slab 1, ..., then the y container
 //   main stream:  slab k of the row-slab forward as soon as its rows are in
-//                 (slab 0 in store mode into a fresh device y), then y += the
+//                 (slab 0 in store mode into a fresh device y), the heights
+//                 of a 4-height remainder once all rows are in, then y += the
 //                 container, then y back to the host
 // The volume arrives while earlier slabs project, and the container while
 // the projection runs; only the first slab's rows and the result's way back
@@ -218,6 +219,7 @@ cudaError_t forward_z0_host(const float* x_host, float* y_host, const float* ang
       VP_TRY(launch_forward_z0_row_slab(xd, yd, ad, gs, k, s));
       *launches += forward_z0_row_slab_launches(xd, yd, g);
     }
+    VP_TRY(launch_forward_z0_row_rest(xd, yd, ad, gs, s, launches));
     VP_TRY(cudaStreamWaitEvent(s, ev_cont, 0));
     if (g.accumulate) {
       VP_TRY(launch_add(yd, yc, y_elems, s));
@@ -277,7 +279,7 @@ cudaError_t backward_z0_host(const float* y_host, float* x_host, const float* an
       const int lo = k * rows;
       const int hi = lo + rows < g.SY ? lo + rows : g.SY;
       VP_TRY(launch_backward_z0_rows(yd, xd, ad, gs, lo, hi, s));
-      *launches += (lo == 0 && hi == g.SY) ? launches_backward_z0(yd, xd, g) : 2;
+      *launches += launches_backward_z0(yd, xd, g);
       VP_TRY(cudaEventRecord(ev_rows[k], s));
       // rows [lo, hi) are final: add the container's rows and send them back
       VP_TRY(cudaStreamWaitEvent(c->copy_out, ev_rows[k], 0));

@@ -40,10 +40,31 @@ cudaError_t forward_z2_transposed(const float* x, float* y, const float* angles,
 cudaError_t backward_z2_transposed(const float* y, float* x, const float* angles, const Geom& g,
                                    float* ws, cudaStream_t stream);
 
+// Height split of the 8-heights-per-lane forms: heights [0, r8_heights(H))
+// run with 8 per lane (chunks of 256); a last chunk of at most 128 heights
+// runs with 4 per lane instead, since 8 would leave half of it idle.
+inline int r8_heights(int H) {
+  const int full = H / 256 * 256;
+  return (H - full > 128 || full == 0) ? H : full;
+}
+
+// Forward launch plan of a kernel variant (0 = default) for a geometry:
+// heights per lane R, bins per warp KW, candidates in flight un, block on
+// neighbouring angles, class slabs, and nslabs slabs of wy rows (and wx
+// columns for class slabs; slab k as detail::slab_of).  The batched kernel
+// follows the same plan, so its results equal the single-problem kernel's.
+struct Fp0Plan {
+  int R, KW, un;
+  bool agroup, cls;
+  int nslabs, wy, wx;
+};
+Fp0Plan forward_z0_plan(const Geom& g, bool vec4, int variant);
+
 // Streamed forms for host buffers.  Forward: the selected variant in row
 // slabs; slab k reads only volume rows [row_lo, row_hi), and launching slabs
-// 0..n-1 in order (slab 0 in g.accumulate's mode, later ones adding) gives
-// the full result.  Adjoint: voxel rows [row_lo, row_hi) alone, row_lo a
+// 0..n-1 in order (slab 0 in g.accumulate's mode, later ones adding), then
+// the rest (a 4-height remainder of split heights, if any), gives the full
+// result.  Adjoint: voxel rows [row_lo, row_hi) alone, row_lo a
 // multiple of backward_z0_row_step() (0: rows cannot be split, launch
 // [0, SY) only).
 int forward_z0_row_slabs(const float* x, const float* y, const Geom& g);
@@ -52,6 +73,8 @@ void forward_z0_row_slab(const float* x, const float* y, const Geom& g, int k, i
 cudaError_t launch_forward_z0_row_slab(const float* x, float* y, const float* angles,
                                        const Geom& g, int k, cudaStream_t stream);
 int forward_z0_row_slab_launches(const float* x, const float* y, const Geom& g);
+cudaError_t launch_forward_z0_row_rest(const float* x, float* y, const float* angles,
+                                       const Geom& g, cudaStream_t stream, int* launches);
 int backward_z0_row_step(const float* y, const float* x, const Geom& g);
 cudaError_t launch_backward_z0_rows(const float* y, float* x, const float* angles,
                                     const Geom& g, int row_lo, int row_hi,

@@ -6,9 +6,10 @@ so a shape is timed once per machine.  The time of every kernel is linear in
 the angle count, so shapes are tuned with at most 90 angles.
 
 Two consumers:
-* ``batch_variant(op, side, n_ang)`` chooses the work-item body of a batched
-  problem (adjoint: runs in two angle classes or 2x2 voxel blocks; the
-  forward has one body), timed as a one-problem batch;
+* ``batch_variant(op, side, n_ang)`` chooses the work-item body and slab
+  plan of a batched problem (forward: 8 heights per lane with class slabs or
+  4 with row slabs; adjoint: runs with 8 or 4 heights per lane, or 2x2 voxel
+  blocks), timed as a one-problem batch;
 * ``tune_single(op, x_shape, y_shape)`` chooses the single-problem kernel
   variant and applies it with ``vp_set_kernel_variant``.
 
@@ -26,7 +27,7 @@ import torch
 
 from . import _lib
 
-BATCH_CANDIDATES = {"forward": [1], "backward": [6, 4]}
+BATCH_CANDIDATES = {"forward": [10, 1], "backward": [7, 6, 4]}
 SINGLE_CANDIDATES = {"forward": [10, 11, 7, 1], "backward": [7, 6, 4, 1]}
 TUNE_ANGLES = 90
 

@@ -211,53 +211,73 @@ int launches_forward_z2(const Geom& g) {
   return (int)ceil_div(g.n_ang, (long long)kMaxGridYZ * FP2_WARPS);
 }
 
-// Slabs [k0, k1) of the configuration's nslabs.
+// One slab launch: slab, the caller's mode for it, and the angles [a_lo, a_hi)
+// (the kernels index angles and y absolutely; g.n_ang is set to a_hi for
+// their bound check).
+struct SlabLaunch {
+  const float* x;
+  float* y;
+  const float* angles;
+  Geom g;
+  Slab slab;
+  int accumulate;
+  int a_lo, a_hi;
+};
+
 template <int R, int KW, bool AGROUP, int UN>
-cudaError_t launch_fp_z0(const float* x, float* y, const float* angles, const Geom& g,
-                         const Fp0Config& c, int k0, int k1, cudaStream_t stream) {
-  const int nslabs = fp0_slabs(g, c);
+cudaError_t launch_slab(const SlabLaunch& L, cudaStream_t stream, int* launches) {
   dim3 block(32, FP0_WARPS);
-  const long long angles_per_launch = AGROUP ? (long long)kMaxGridYZ * FP0_WARPS : kMaxGridYZ;
-  for (int k = k0; k < k1 && k < nslabs; ++k) {
-    const Slab slab = fp0_slab(g, c, k, nslabs);
-    // the first slab applies the caller's mode; later slabs add to it
-    const int accumulate = k == 0 ? g.accumulate : 1;
-    for (long long a_base = 0; a_base < g.n_ang; a_base += angles_per_launch) {
-      const long long na = g.n_ang - a_base < angles_per_launch ? g.n_ang - a_base
-                                                                 : angles_per_launch;
-      const unsigned gx = AGROUP ? ceil_div(g.PX, KW) : ceil_div(g.PX, KW * FP0_WARPS);
-      const unsigned gy = AGROUP ? ceil_div(na, FP0_WARPS) : (unsigned)na;
-      dim3 grid(gx, gy, ceil_div(g.H, 32 * R));
-      fp_z0_kernel<R, KW, AGROUP, UN><<<grid, block, 0, stream>>>(x, y, angles, g,
-                                                                  (int)a_base, slab,
-                                                                  accumulate);
-      const cudaError_t e = cudaGetLastError();
-      if (e != cudaSuccess) return e;
-    }
+  const long long per_launch = AGROUP ? (long long)kMaxGridYZ * FP0_WARPS : kMaxGridYZ;
+  Geom g = L.g;
+  g.n_ang = L.a_hi;
+  for (long long a_base = L.a_lo; a_base < L.a_hi; a_base += per_launch) {
+    const long long na = L.a_hi - a_base < per_launch ? L.a_hi - a_base : per_launch;
+    const unsigned gx = AGROUP ? ceil_div(g.PX, KW) : ceil_div(g.PX, KW * FP0_WARPS);
+    const unsigned gy = AGROUP ? ceil_div(na, FP0_WARPS) : (unsigned)na;
+    dim3 grid(gx, gy, ceil_div(g.H, 32 * R));
+    fp_z0_kernel<R, KW, AGROUP, UN><<<grid, block, 0, stream>>>(L.x, L.y, L.angles, g,
+                                                                (int)a_base, L.slab,
+                                                                L.accumulate);
+    if (launches) ++*launches;
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
   }
   return cudaSuccess;
 }
 
 template <int R>
-cudaError_t launch_fp_z0_r(const float* x, float* y, const float* angles, const Geom& g,
-                           const Fp0Config& c, int k0, int k1, cudaStream_t stream) {
+cudaError_t launch_slab_r(const Fp0Config& c, const SlabLaunch& L, cudaStream_t s, int* n) {
   if (c.KW == 8) {
-    if (c.agroup) return launch_fp_z0<R, 8, true, FP0_UNROLL>(x, y, angles, g, c, k0, k1, stream);
-    return launch_fp_z0<R, 8, false, FP0_UNROLL>(x, y, angles, g, c, k0, k1, stream);
+    if (c.agroup) return launch_slab<R, 8, true, FP0_UNROLL>(L, s, n);
+    return launch_slab<R, 8, false, FP0_UNROLL>(L, s, n);
   }
-  if (c.agroup) return launch_fp_z0<R, 4, true, FP0_UNROLL>(x, y, angles, g, c, k0, k1, stream);
-  return launch_fp_z0<R, 4, false, FP0_UNROLL>(x, y, angles, g, c, k0, k1, stream);
+  if (c.agroup) return launch_slab<R, 4, true, FP0_UNROLL>(L, s, n);
+  return launch_slab<R, 4, false, FP0_UNROLL>(L, s, n);
 }
 
-cudaError_t launch_fp_z0_config(const float* x, float* y, const float* angles, const Geom& g,
-                                const Fp0Config& c, int k0, int k1, cudaStream_t stream) {
+cudaError_t launch_slab_config(const Fp0Config& c, const SlabLaunch& L, cudaStream_t s, int* n) {
   if (c.R == 8) {
-    if (c.KW == 8) return launch_fp_z0<8, 8, false, 2>(x, y, angles, g, c, k0, k1, stream);
-    if (c.un == 2) return launch_fp_z0<8, 4, false, 2>(x, y, angles, g, c, k0, k1, stream);
-    return launch_fp_z0<8, 4, false, 4>(x, y, angles, g, c, k0, k1, stream);
+    if (c.KW == 8) return launch_slab<8, 8, false, 2>(L, s, n);
+    if (c.un == 2) return launch_slab<8, 4, false, 2>(L, s, n);
+    return launch_slab<8, 4, false, 4>(L, s, n);
   }
-  if (c.R == 4) return launch_fp_z0_r<4>(x, y, angles, g, c, k0, k1, stream);
-  return launch_fp_z0_r<1>(x, y, angles, g, c, k0, k1, stream);
+  if (c.R == 4) return launch_slab_r<4>(c, L, s, n);
+  return launch_slab_r<1>(c, L, s, n);
+}
+
+// Slabs [k0, k1) of the configuration's plan, all angles; the first slab
+// applies the caller's mode, later slabs add to it.
+cudaError_t launch_fp_z0_config(const float* x, float* y, const float* angles, const Geom& g,
+                                const Fp0Config& c, int k0, int k1, cudaStream_t stream,
+                                int* launches = nullptr) {
+  const int nslabs = fp0_slabs(g, c);
+  for (int k = k0; k < k1 && k < nslabs; ++k) {
+    const SlabLaunch L{x, y, angles, g, fp0_slab(g, c, k, nslabs), k == 0 ? g.accumulate : 1,
+                       0, g.n_ang};
+    const cudaError_t e = launch_slab_config(c, L, stream, launches);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
 }
 
 // The heights of a call as (first height, count) parts: one part, or with 8
@@ -322,57 +342,56 @@ int launches_forward_z0(const float* x, const float* y, const Geom& g) {
   return n;
 }
 
-// Row-slab form of the selected variant, for volumes that arrive in row
-// order: slab k of the main height part reads only rows
-// [forward_z0_row_slab(k)); the 4-height remainder of a split (if any) runs
-// whole once every row is in (launch_forward_z0_row_rest).
-Fp0Config fp0_stream_config(const Geom& g, bool vec4) {
-  Fp0Config c = fp0_config(g, vec4, kernel_variant(OP_FORWARD_Z0));
+// Streamed form for volumes that arrive in row order, on the main height
+// part (launch_forward_z0_stream): while rows arrive, angles whose minor axis
+// is x walk the rows that are in (the other class's range is empty); once
+// all are in, the other angles walk blocks of columns.  Together these are
+// the class slabs of the device path, spread over time.  The 4-height
+// remainder of a split heights range runs whole at the end
+// (launch_forward_z0_rest).
+int forward_z0_stream_rows(const float* x, const float* y, const Geom& g) {
+  const bool vec4 = fp0_vec4(x, y, g);
+  const int v = kernel_variant(OP_FORWARD_Z0);
+  const Geom gm = fp0_parts(g, vec4, v).g[0];
+  Fp0Config c = fp0_config(gm, vec4, v);
+  c.cls = false;  // rows of one class alone: the row-slab budget
+  return fp0_slab_rows(gm, c);
+}
+
+int forward_z0_stream_cols(const float* x, const float* y, const Geom& g) {
+  const bool vec4 = fp0_vec4(x, y, g);
+  const int v = kernel_variant(OP_FORWARD_Z0);
+  const Geom gm = fp0_parts(g, vec4, v).g[0];
+  Fp0Config c = fp0_config(gm, vec4, v);
   c.cls = false;
-  return c;
+  Geom gt = gm;  // columns of the other class: rows and columns swapped
+  gt.SY = gm.SX;
+  gt.SX = gm.SY;
+  return fp0_slab_rows(gt, c);
 }
 
-Geom fp0_stream_main(const float* x, const float* y, const Geom& g) {
-  return fp0_parts(g, fp0_vec4(x, y, g), kernel_variant(OP_FORWARD_Z0)).g[0];
+cudaError_t launch_forward_z0_stream(const float* x, float* y, const float* angles,
+                                     const Geom& g, int rows_lo, int rows_hi, int cols_lo,
+                                     int cols_hi, int a_lo, int a_hi, int accumulate,
+                                     cudaStream_t stream, int* launches) {
+  const bool vec4 = fp0_vec4(x, y, g);
+  const int v = kernel_variant(OP_FORWARD_Z0);
+  const Geom gm = fp0_parts(g, vec4, v).g[0];
+  Fp0Config c = fp0_config(gm, vec4, v);
+  c.cls = true;
+  const SlabLaunch L{x, y, angles, gm, Slab{rows_lo, rows_hi, cols_lo, cols_hi, 0, g.SY},
+                     accumulate, a_lo, a_hi};
+  return launch_slab_config(c, L, stream, launches);
 }
 
-int forward_z0_row_slabs(const float* x, const float* y, const Geom& g) {
-  const Geom gm = fp0_stream_main(x, y, g);
-  return fp0_slabs(gm, fp0_stream_config(gm, fp0_vec4(x, y, g)));
-}
-
-void forward_z0_row_slab(const float* x, const float* y, const Geom& g, int k, int* row_lo,
-                         int* row_hi) {
-  const Geom gm = fp0_stream_main(x, y, g);
-  const Fp0Config c = fp0_stream_config(gm, fp0_vec4(x, y, g));
-  const Slab s = fp0_slab(gm, c, k, fp0_slabs(gm, c));
-  *row_lo = s.y_lo;
-  *row_hi = s.y_hi;
-}
-
-cudaError_t launch_forward_z0_row_slab(const float* x, float* y, const float* angles,
-                                       const Geom& g, int k, cudaStream_t stream) {
-  const Geom gm = fp0_stream_main(x, y, g);
-  return launch_fp_z0_config(x, y, angles, gm, fp0_stream_config(gm, fp0_vec4(x, y, g)), k,
-                             k + 1, stream);
-}
-
-int forward_z0_row_slab_launches(const float* x, const float* y, const Geom& g) {
-  const Geom gm = fp0_stream_main(x, y, g);
-  const Fp0Config c = fp0_stream_config(gm, fp0_vec4(x, y, g));
-  return (int)ceil_div(g.n_ang, c.agroup ? (long long)kMaxGridYZ * FP0_WARPS : kMaxGridYZ);
-}
-
-cudaError_t launch_forward_z0_row_rest(const float* x, float* y, const float* angles,
-                                       const Geom& g, cudaStream_t stream, int* launches) {
+cudaError_t launch_forward_z0_rest(const float* x, float* y, const float* angles,
+                                   const Geom& g, cudaStream_t stream, int* launches) {
   const bool vec4 = fp0_vec4(x, y, g);
   const HeightParts hp = fp0_parts(g, vec4, kernel_variant(OP_FORWARD_Z0));
   if (hp.n < 2) return cudaSuccess;
-  const Fp0Config c = fp0_stream_config(hp.g[1], vec4);
-  *launches += fp0_slabs(hp.g[1], c) *
-               (int)ceil_div(g.n_ang, c.agroup ? (long long)kMaxGridYZ * FP0_WARPS : kMaxGridYZ);
+  const Fp0Config c = fp0_config(hp.g[1], vec4, kernel_variant(OP_FORWARD_Z0));
   return launch_fp_z0_config(x + hp.h0[1], y + hp.h0[1], angles, hp.g[1], c, 0, 1 << 30,
-                             stream);
+                             stream, launches);
 }
 
 cudaError_t launch_forward_z2(const float* x, float* y, const float* angles, const Geom& g,

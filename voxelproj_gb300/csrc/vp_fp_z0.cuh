@@ -94,6 +94,8 @@ __device__ __forceinline__ void scatter_q(V (&acc)[KW], const float4& e, const V
 //   row slabs:   {y_lo, y_hi, 0, SX, y_lo, y_hi}  (one block of rows for all)
 //   class slabs: {y_lo, y_hi, x_lo, x_hi, 0, SY}  (rows for one class,
 //                                                  columns for the other)
+// An empty range leaves that class's outputs untouched when adding (and
+// writes zeros in store mode), so a launch can serve one class alone.
 struct Slab {
   int y_lo, y_hi;
   int x_lo, x_hi;
@@ -141,6 +143,10 @@ __device__ __forceinline__ void fp_z0_warp(const float* __restrict__ x, float* _
   // major lines [maj_lo, maj_hi), minor indices [min_lo, min_hi], within the slab
   const int maj_lo = minor_x ? s.y_lo : s.x_lo;
   const int maj_hi = minor_x ? s.y_hi : s.x_hi;
+  if (maj_lo >= maj_hi && accumulate) {  // warp-uniform: nothing of this slab to add
+    wait();
+    return;
+  }
   const int min_lo = minor_x ? 0 : s.yy_lo;
   const int min_hi = minor_x ? g.SX - 1 : s.yy_hi - 1;
   const float cent_major = minor_x ? g.ycent : g.xcent;

@@ -1,22 +1,28 @@
 // Host-buffer projections (z_order 0): the caller's arrays stay in host
 // memory, and the copies to and from the device overlap the kernels.
 //
-// Forward, y_host (+)= A x_host:
-//   copy stream:  angles, x rows of slab 0, slab 1, ..., then the y container
-//   main stream:  slab k of the row-slab forward as soon as its rows are in
-//                 (slab 0 in store mode into a fresh device y), the heights
-//                 of a 4-height remainder once all rows are in, then y += the
-//                 container, then y back to the host
-// The volume arrives while earlier slabs project, and the container while
-// the projection runs; only the first slab's rows and the result's way back
-// are exposed.
+// Forward, y_host (+)= A x_host, on row slabs of the forward's plan:
+//   copy stream:  angles, the volume's rows piece by piece (a quarter of a
+//                 slab first, so that the kernels start early), then the y
+//                 container
+//   main stream:  angles whose minor axis is x, on each piece of rows as
+//                 soon as it is in (the first launch in store mode into a
+//                 fresh device y); once all rows are in, a 4-height remainder
+//                 of split heights, then the other angles on blocks of
+//                 columns, the last block in angle groups
+//   out stream:   per angle group, once final: y rows of those angles +=
+//                 container, and back to the host
 //
 // Adjoint, x_host (+)= A^T y_host:
-//   copy stream:  angles, y, then the x container
-//   main stream:  the adjoint of voxel rows [r_k, r_k+1) per slab, in store
-//                 mode into a fresh device x
-//   out stream:   per slab, once computed: x rows += container rows, rows back
-// The result leaves the device while later rows are still being computed.
+//   copy stream:  angles, the first quarter of the angles' sinogram rows,
+//                 the rest, then the x container slab by slab
+//   main stream:  the adjoint of the first angles over the whole volume as
+//                 soon as they are in (store mode into a fresh device x),
+//                 then the remaining angles in row slabs, alternating with a
+//                 second kernel stream so that one slab's last wave overlaps
+//                 the next slab
+//   out stream:   per row slab, once computed: x rows += container rows,
+//                 and back to the host
 //
 // Device buffers come from the library's stream-ordered pool, so repeated
 // calls reuse memory without going back to the driver.  Copies use
@@ -40,13 +46,14 @@ namespace vp {
 namespace {
 
 constexpr int kMaxDevices = 64;
-// Adjoint slabs: about this many rows of output each (and at least RUN).
-constexpr int kAdjointSlabs = 8;
+constexpr int kAdjointSlabs = 8;      // adjoint row slabs per call
+constexpr int kForwardAngleGroups = 4;  // groups of the forward's last slab
 
 // Side streams and events of one device, created on first use and kept.
 struct HostCtx {
   cudaStream_t copy_in = nullptr;
   cudaStream_t copy_out = nullptr;
+  cudaStream_t compute2 = nullptr;  // a second kernel stream for independent slabs
   std::vector<cudaEvent_t> ev;
 };
 std::mutex g_mutex;  // one host-buffer call per process at a time
@@ -62,6 +69,8 @@ cudaError_t get_ctx(int nev, HostCtx** out) {
     if ((e = cudaStreamCreateWithFlags(&c.copy_in, cudaStreamNonBlocking)) != cudaSuccess)
       return e;
     if ((e = cudaStreamCreateWithFlags(&c.copy_out, cudaStreamNonBlocking)) != cudaSuccess)
+      return e;
+    if ((e = cudaStreamCreateWithFlags(&c.compute2, cudaStreamNonBlocking)) != cudaSuccess)
       return e;
   }
   while ((int)c.ev.size() < nev) {
@@ -161,6 +170,7 @@ cudaError_t guarded(F body, cudaStream_t s) {
         g_ctx[dev].copy_in != nullptr) {
       cudaStreamSynchronize(g_ctx[dev].copy_in);
       cudaStreamSynchronize(g_ctx[dev].copy_out);
+      cudaStreamSynchronize(g_ctx[dev].compute2);
     }
     cudaStreamSynchronize(s);
   }
@@ -174,7 +184,8 @@ cudaError_t forward_z0_host(const float* x_host, float* y_host, const float* ang
   std::lock_guard<std::mutex> lock(g_mutex);
   const size_t row_elems = (size_t)g.SX * g.Hx;
   const size_t x_elems = (size_t)g.SY * row_elems;
-  const size_t y_elems = (size_t)g.n_ang * g.PX * g.Hy;
+  const size_t ang_elems = (size_t)g.PX * g.Hy;  // one angle of y
+  const size_t y_elems = (size_t)g.n_ang * ang_elems;
   Buffers buf(s);
   return guarded([&]() -> cudaError_t {
     float *xd = nullptr, *yd = nullptr, *yc = nullptr, *as = nullptr;
@@ -183,30 +194,54 @@ cudaError_t forward_z0_host(const float* x_host, float* y_host, const float* ang
     VP_TRY(buf.get(pool, y_elems * sizeof(float), &yd));
     if (g.accumulate) VP_TRY(buf.get(pool, y_elems * sizeof(float), &yc));
     VP_TRY(alloc_angles(angles, g, buf, pool, &ad, &as));
-    // the slab plan depends on the device buffers' alignment, which is 16 bytes
-    const int nslabs = forward_z0_row_slabs(xd, yd, g);
+    // row pieces: a quarter slab, the rest of the first slab, then whole
+    // slabs of the plan (which depends on the device buffers' alignment);
+    // column pieces of the plan
+    const int rows = forward_z0_stream_rows(xd, yd, g);
+    const int cols = forward_z0_stream_cols(xd, yd, g);
+    std::vector<int> cut{0};
+    const int quarter = rows / 4 >= 8 ? rows / 4 : rows;
+    int r = quarter < g.SY ? quarter : g.SY;
+    cut.push_back(r);
+    if (r < g.SY && r < rows) {  // the rest of the first slab
+      r = rows < g.SY ? rows : g.SY;
+      cut.push_back(r);
+    }
+    while (r < g.SY) {
+      r = r + rows < g.SY ? r + rows : g.SY;
+      cut.push_back(r);
+    }
+    std::vector<int> ccut{0};
+    for (int q = 0; q < g.SX;) {
+      q = q + cols < g.SX ? q + cols : g.SX;
+      ccut.push_back(q);
+    }
+    const int npieces = (int)cut.size() - 1;
+    const int ncpieces = (int)ccut.size() - 1;
+    const int ngroups = g.n_ang < kForwardAngleGroups ? g.n_ang : kForwardAngleGroups;
     HostCtx* c = nullptr;
-    VP_TRY(get_ctx(nslabs + 2, &c));
-    cudaEvent_t ev_alloc = c->ev[0], ev_cont = c->ev[1];
-    cudaEvent_t* ev_slab = c->ev.data() + 2;
+    VP_TRY(get_ctx(npieces + ngroups + 3, &c));
+    cudaEvent_t ev_alloc = c->ev[0], ev_cont = c->ev[1], ev_out = c->ev[2];
+    cudaEvent_t* ev_piece = c->ev.data() + 3;
+    cudaEvent_t* ev_group = ev_piece + npieces;
 
-    // the copy stream starts after the allocations (and prior work) on s
+    // the side streams start after the allocations (and prior work) on s
     VP_TRY(cudaEventRecord(ev_alloc, s));
     VP_TRY(cudaStreamWaitEvent(c->copy_in, ev_alloc, 0));
+    VP_TRY(cudaStreamWaitEvent(c->copy_out, ev_alloc, 0));
     VP_TRY(copy_angles(as, angles, g, c->copy_in));
-    for (int k = 0; k < nslabs; ++k) {
-      int lo = 0, hi = 0;
-      forward_z0_row_slab(xd, yd, g, k, &lo, &hi);
-      if (hi > lo)
-        VP_TRY(cudaMemcpyAsync(xd + (size_t)lo * row_elems, x_host + (size_t)lo * row_elems,
-                               (size_t)(hi - lo) * row_elems * sizeof(float),
-                               cudaMemcpyDefault, c->copy_in));
-      VP_TRY(cudaEventRecord(ev_slab[k], c->copy_in));
+    for (int k = 0; k < npieces; ++k) {
+      const size_t off = (size_t)cut[k] * row_elems;
+      VP_TRY(cudaMemcpyAsync(xd + off, x_host + off,
+                             (size_t)(cut[k + 1] - cut[k]) * row_elems * sizeof(float),
+                             cudaMemcpyDefault, c->copy_in));
+      VP_TRY(cudaEventRecord(ev_piece[k], c->copy_in));
     }
     if (g.accumulate)
       VP_TRY(cudaMemcpyAsync(yc, y_host, y_elems * sizeof(float), cudaMemcpyDefault,
                              c->copy_in));
     VP_TRY(cudaEventRecord(ev_cont, c->copy_in));
+    VP_TRY(cudaStreamWaitEvent(c->copy_out, ev_cont, 0));
 
     Geom gs = g;
     gs.accumulate = 0;
@@ -214,18 +249,36 @@ cudaError_t forward_z0_host(const float* x_host, float* y_host, const float* ang
       VP_TRY(cudaMemsetAsync(yd, 0, y_elems * sizeof(float), s));
       gs.accumulate = 1;
     }
-    for (int k = 0; k < nslabs; ++k) {
-      VP_TRY(cudaStreamWaitEvent(s, ev_slab[k], 0));
-      VP_TRY(launch_forward_z0_row_slab(xd, yd, ad, gs, k, s));
-      *launches += forward_z0_row_slab_launches(xd, yd, g);
+    // angles whose minor axis is x, on each piece of rows as it arrives
+    for (int k = 0; k < npieces; ++k) {
+      VP_TRY(cudaStreamWaitEvent(s, ev_piece[k], 0));
+      VP_TRY(launch_forward_z0_stream(xd, yd, ad, gs, cut[k], cut[k + 1], 0, 0, 0, g.n_ang,
+                                      k == 0 ? gs.accumulate : 1, s, launches));
     }
-    VP_TRY(launch_forward_z0_row_rest(xd, yd, ad, gs, s, launches));
-    VP_TRY(cudaStreamWaitEvent(s, ev_cont, 0));
-    if (g.accumulate) {
-      VP_TRY(launch_add(yd, yc, y_elems, s));
-      *launches += 1;
+    // every row is in: the remainder heights, then the other angles on blocks
+    // of columns; the last block by angle groups, each group sent back once
+    // final
+    VP_TRY(launch_forward_z0_rest(xd, yd, ad, gs, s, launches));
+    for (int j = 0; j + 1 < ncpieces; ++j)
+      VP_TRY(launch_forward_z0_stream(xd, yd, ad, gs, 0, 0, ccut[j], ccut[j + 1], 0, g.n_ang, 1,
+                                      s, launches));
+    for (int j = 0; j < ngroups; ++j) {
+      const int a0 = (int)((long long)g.n_ang * j / ngroups);
+      const int a1 = (int)((long long)g.n_ang * (j + 1) / ngroups);
+      VP_TRY(launch_forward_z0_stream(xd, yd, ad, gs, 0, 0, ccut[ncpieces - 1],
+                                      ccut[ncpieces], a0, a1, 1, s, launches));
+      VP_TRY(cudaEventRecord(ev_group[j], s));
+      VP_TRY(cudaStreamWaitEvent(c->copy_out, ev_group[j], 0));
+      const size_t off = (size_t)a0 * ang_elems, n = (size_t)(a1 - a0) * ang_elems;
+      if (g.accumulate) {
+        VP_TRY(launch_add(yd + off, yc + off, n, c->copy_out));
+        *launches += 1;
+      }
+      VP_TRY(cudaMemcpyAsync(y_host + off, yd + off, n * sizeof(float), cudaMemcpyDefault,
+                             c->copy_out));
     }
-    return cudaMemcpyAsync(y_host, yd, y_elems * sizeof(float), cudaMemcpyDefault, s);
+    VP_TRY(cudaEventRecord(ev_out, c->copy_out));
+    return cudaStreamWaitEvent(s, ev_out, 0);  // s ends after the last angles are home
   }, s);
 }
 
@@ -234,7 +287,8 @@ cudaError_t backward_z0_host(const float* y_host, float* x_host, const float* an
   std::lock_guard<std::mutex> lock(g_mutex);
   const size_t row_elems = (size_t)g.SX * g.Hx;
   const size_t x_elems = (size_t)g.SY * row_elems;
-  const size_t y_elems = (size_t)g.n_ang * g.PX * g.Hy;
+  const size_t ang_elems = (size_t)g.PX * g.Hy;
+  const size_t y_elems = (size_t)g.n_ang * ang_elems;
   Buffers buf(s);
   return guarded([&]() -> cudaError_t {
     float *xd = nullptr, *yd = nullptr, *xc = nullptr, *as = nullptr;
@@ -251,21 +305,36 @@ cudaError_t backward_z0_host(const float* y_host, float* x_host, const float* an
       rows = (rows + step - 1) / step * step;
     }
     const int nslabs = (g.SY + rows - 1) / rows;
+    // the first quarter of the angles runs over the whole volume first
+    const int a_split = g.n_ang >= 8 ? g.n_ang / 4 : 0;
     HostCtx* c = nullptr;
-    VP_TRY(get_ctx(nslabs + 4, &c));
-    cudaEvent_t ev_alloc = c->ev[0], ev_in = c->ev[1], ev_cont = c->ev[2], ev_out = c->ev[3];
-    cudaEvent_t* ev_rows = c->ev.data() + 4;
+    VP_TRY(get_ctx(2 * nslabs + 6, &c));
+    cudaEvent_t ev_alloc = c->ev[0], ev_in0 = c->ev[1], ev_in = c->ev[2], ev_out = c->ev[3],
+                ev_first = c->ev[4], ev_c2 = c->ev[5];
+    cudaEvent_t* ev_rows = c->ev.data() + 6;
+    cudaEvent_t* ev_cont = ev_rows + nslabs;  // container rows of slab k are in
 
     VP_TRY(cudaEventRecord(ev_alloc, s));
     VP_TRY(cudaStreamWaitEvent(c->copy_in, ev_alloc, 0));
     VP_TRY(cudaStreamWaitEvent(c->copy_out, ev_alloc, 0));
     VP_TRY(copy_angles(as, angles, g, c->copy_in));
-    VP_TRY(cudaMemcpyAsync(yd, y_host, y_elems * sizeof(float), cudaMemcpyDefault, c->copy_in));
+    const size_t y0 = (size_t)a_split * ang_elems;
+    if (y0 > 0)
+      VP_TRY(cudaMemcpyAsync(yd, y_host, y0 * sizeof(float), cudaMemcpyDefault, c->copy_in));
+    VP_TRY(cudaEventRecord(ev_in0, c->copy_in));
+    VP_TRY(cudaMemcpyAsync(yd + y0, y_host + y0, (y_elems - y0) * sizeof(float),
+                           cudaMemcpyDefault, c->copy_in));
     VP_TRY(cudaEventRecord(ev_in, c->copy_in));
-    if (g.accumulate)
-      VP_TRY(cudaMemcpyAsync(xc, x_host, x_elems * sizeof(float), cudaMemcpyDefault,
-                             c->copy_in));
-    VP_TRY(cudaEventRecord(ev_cont, c->copy_in));
+    // the container slab by slab, in the order the results leave
+    for (int k = 0; k < nslabs; ++k) {
+      const int lo = k * rows;
+      const int hi = lo + rows < g.SY ? lo + rows : g.SY;
+      const size_t off = (size_t)lo * row_elems;
+      if (g.accumulate)
+        VP_TRY(cudaMemcpyAsync(xc + off, x_host + off, (size_t)(hi - lo) * row_elems *
+                               sizeof(float), cudaMemcpyDefault, c->copy_in));
+      VP_TRY(cudaEventRecord(ev_cont[k], c->copy_in));
+    }
 
     Geom gs = g;
     gs.accumulate = 0;
@@ -273,16 +342,30 @@ cudaError_t backward_z0_host(const float* y_host, float* x_host, const float* an
       VP_TRY(cudaMemsetAsync(xd, 0, x_elems * sizeof(float), s));
       gs.accumulate = 1;
     }
+    // angles [0, a_split) over all rows; then angles [a_split, n) by row slabs
+    Geom g1 = gs;
+    if (a_split > 0) {
+      Geom g0 = gs;
+      g0.n_ang = a_split;
+      VP_TRY(cudaStreamWaitEvent(s, ev_in0, 0));
+      VP_TRY(launch_backward_z0_rows(yd, xd, ad, g0, 0, g.SY, s));
+      *launches += launches_backward_z0(yd, xd, g0);
+      g1.n_ang = g.n_ang - a_split;
+      g1.accumulate = 1;
+    }
     VP_TRY(cudaStreamWaitEvent(s, ev_in, 0));
-    VP_TRY(cudaStreamWaitEvent(c->copy_out, ev_cont, 0));
+    VP_TRY(cudaEventRecord(ev_first, s));  // y is in and the first angles are launched
+    VP_TRY(cudaStreamWaitEvent(c->compute2, ev_first, 0));
     for (int k = 0; k < nslabs; ++k) {
       const int lo = k * rows;
       const int hi = lo + rows < g.SY ? lo + rows : g.SY;
-      VP_TRY(launch_backward_z0_rows(yd, xd, ad, gs, lo, hi, s));
-      *launches += launches_backward_z0(yd, xd, g);
-      VP_TRY(cudaEventRecord(ev_rows[k], s));
+      const cudaStream_t sk = (k & 1) ? c->compute2 : s;  // slabs write disjoint rows
+      VP_TRY(launch_backward_z0_rows(yd + y0, xd, ad + a_split, g1, lo, hi, sk));
+      *launches += launches_backward_z0(yd, xd, g1);
+      VP_TRY(cudaEventRecord(ev_rows[k], sk));
       // rows [lo, hi) are final: add the container's rows and send them back
       VP_TRY(cudaStreamWaitEvent(c->copy_out, ev_rows[k], 0));
+      VP_TRY(cudaStreamWaitEvent(c->copy_out, ev_cont[k], 0));
       const size_t off = (size_t)lo * row_elems, n = (size_t)(hi - lo) * row_elems;
       if (g.accumulate) {
         VP_TRY(launch_add(xd + off, xc + off, n, c->copy_out));
@@ -291,6 +374,8 @@ cudaError_t backward_z0_host(const float* y_host, float* x_host, const float* an
       VP_TRY(cudaMemcpyAsync(x_host + off, xd + off, n * sizeof(float), cudaMemcpyDefault,
                              c->copy_out));
     }
+    VP_TRY(cudaEventRecord(ev_c2, c->compute2));
+    VP_TRY(cudaStreamWaitEvent(s, ev_c2, 0));
     VP_TRY(cudaEventRecord(ev_out, c->copy_out));
     return cudaStreamWaitEvent(s, ev_out, 0);  // s ends after the last row is home
   }, s);

@@ -60,21 +60,25 @@ struct Fp0Plan {
 };
 Fp0Plan forward_z0_plan(const Geom& g, bool vec4, int variant);
 
-// Streamed forms for host buffers.  Forward: the selected variant in row
-// slabs; slab k reads only volume rows [row_lo, row_hi), and launching slabs
-// 0..n-1 in order (slab 0 in g.accumulate's mode, later ones adding), then
-// the rest (a 4-height remainder of split heights, if any), gives the full
-// result.  Adjoint: voxel rows [row_lo, row_hi) alone, row_lo a
-// multiple of backward_z0_row_step() (0: rows cannot be split, launch
-// [0, SY) only).
-int forward_z0_row_slabs(const float* x, const float* y, const Geom& g);
-void forward_z0_row_slab(const float* x, const float* y, const Geom& g, int k, int* row_lo,
-                         int* row_hi);
-cudaError_t launch_forward_z0_row_slab(const float* x, float* y, const float* angles,
-                                       const Geom& g, int k, cudaStream_t stream);
-int forward_z0_row_slab_launches(const float* x, const float* y, const Geom& g);
-cudaError_t launch_forward_z0_row_rest(const float* x, float* y, const float* angles,
-                                       const Geom& g, cudaStream_t stream, int* launches);
+// Streamed forms for host buffers.
+// Forward, on the main height part: launch_forward_z0_stream gathers angles
+// [a_lo, a_hi) from volume rows [rows_lo, rows_hi) for angles whose minor
+// axis is x and from columns [cols_lo, cols_hi) for the others (an empty
+// range skips that class when adding).  Rows in pieces of up to
+// forward_z0_stream_rows (columns empty) as they arrive, then columns in
+// pieces of up to forward_z0_stream_cols (rows empty), the first launch in
+// the caller's mode and the rest adding, then launch_forward_z0_rest (the
+// 4-height remainder of a split heights range, whole), give the full result.
+// Adjoint: voxel rows [row_lo, row_hi) alone, row_lo a multiple of
+// backward_z0_row_step() (0: rows cannot be split, launch [0, SY) only).
+int forward_z0_stream_rows(const float* x, const float* y, const Geom& g);
+int forward_z0_stream_cols(const float* x, const float* y, const Geom& g);
+cudaError_t launch_forward_z0_stream(const float* x, float* y, const float* angles,
+                                     const Geom& g, int rows_lo, int rows_hi, int cols_lo,
+                                     int cols_hi, int a_lo, int a_hi, int accumulate,
+                                     cudaStream_t stream, int* launches);
+cudaError_t launch_forward_z0_rest(const float* x, float* y, const float* angles,
+                                   const Geom& g, cudaStream_t stream, int* launches);
 int backward_z0_row_step(const float* y, const float* x, const Geom& g);
 cudaError_t launch_backward_z0_rows(const float* y, float* x, const float* angles,
                                     const Geom& g, int row_lo, int row_hi,

@@ -85,6 +85,12 @@ VP_API int vp_last_cuda_error(void);
  * GPU launches a sequence of calls issued. */
 VP_API uint64_t vp_launch_count(void);
 
+/* Bounded waits in this library's kernels that ran out since the library was
+ * loaded: 0 in correct operation.  Kernels that wait on asynchronous copies
+ * give up after a bounded time instead of spinning on, count it here and
+ * fall back to direct loads.  Synchronises the device. */
+VP_API uint64_t vp_wait_timeouts(void);
+
 /* Kernel variant selection, used by the autotuner and for measurements.
  * op: 0 = forward z0, 1 = backward z0, 2 = forward z2, 3 = backward z2;
  * variant 0 = automatic (default).  Unknown variants fall back to automatic.

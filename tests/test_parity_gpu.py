@@ -138,7 +138,7 @@ def test_weight_sum_single_voxel():
 # autotuner may pick any of them): sizes that are not multiples of the block
 # or run shape, degenerate angles, both signs of each step, several height
 # chunks.
-@pytest.mark.parametrize("variant", [1, 2, 3, 4, 5, 6, 7])
+@pytest.mark.parametrize("variant", [1, 2, 3, 4, 5, 6, 7, 9])
 @pytest.mark.parametrize("geom", [(23, 37, 132, 61, 50, "wide"), (9, 6, 8, 40, 11, "axes"),
                                   (64, 64, 256, 96, 64, "rand"), (30, 21, 260, 33, 40, "rand")],
                          ids=lambda g: "x".join(map(str, g[:5])) + g[5])
@@ -161,7 +161,7 @@ def test_backward_variants(variant, geom):
     assert err <= tol.ref_vs_fp64(max(SY, SX, PX))
 
 
-@pytest.mark.parametrize("variant", [1, 4, 6, 7])
+@pytest.mark.parametrize("variant", [1, 4, 6, 7, 9])
 @pytest.mark.parametrize("H", [36, 260])
 def test_backward_variants_store_mode_via_z2(variant, H):
     """z_order 2 with H >= 32 runs the z_order 0 kernel in store mode into
@@ -236,3 +236,33 @@ def test_forward_variants_store_mode_via_z2(variant, H):
         _lib.LIB.vp_set_kernel_variant(0, 0)
     np.testing.assert_array_equal(outs[0], outs[1])
     assert rel_err(outs[0] - y0, oracle.forward(x, ang, PX, 2)) <= tol.ref_vs_fp64(PX)
+
+
+@pytest.mark.parametrize("geom", [(48, 40, 512, 70, 52, "wide"), (33, 29, 256, 45, 40, "axes"),
+                                  (40, 44, 772, 300, 47, "rand"), (16, 16, 264, 9, 20, "pi")],
+                         ids=lambda g: "x".join(map(str, g[:5])) + g[5])
+def test_adjoint_bulk_copy_variant_is_bit_identical(geom):
+    """Variant 9 fetches the 8-height windows with bulk copies into shared
+    memory; the arithmetic is variant 7's, so the results are equal bit for
+    bit, and no bounded wait runs out.  Angle counts past one list pass
+    (256) and past one table chunk, windows at the detector edge, heights
+    with a 4-height remainder."""
+    from voxelproj_gb300 import _lib
+
+    SY, SX, H, n, PX, kind = geom
+    ang = torch.tensor(angle_set(kind, n, 97), device="cuda")
+    y = torch.tensor(seeded((n, PX, H), 35), device="cuda")
+    x0 = torch.tensor(seeded((SY, SX, H), 36), device="cuda")
+    before = _lib.LIB.vp_wait_timeouts()
+    outs = {}
+    try:
+        for v in (7, 9):
+            _lib.LIB.vp_set_kernel_variant(1, v)
+            xo = x0.clone()
+            vp._CU.backward_z0(y, xo, ang)
+            torch.cuda.synchronize()
+            outs[v] = xo
+    finally:
+        _lib.LIB.vp_set_kernel_variant(1, 0)
+    assert torch.equal(outs[7], outs[9])
+    assert _lib.LIB.vp_wait_timeouts() == before

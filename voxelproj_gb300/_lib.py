@@ -56,6 +56,7 @@ SIGNATURES = {
     "vp_error_string": (ctypes.c_char_p, [_I]),
     "vp_last_cuda_error": (_I, []),
     "vp_launch_count": (ctypes.c_uint64, []),
+    "vp_wait_timeouts": (ctypes.c_uint64, []),
     "vp_set_kernel_variant": (_I, [_I, _I]),
     "vp_get_kernel_variant": (_I, [_I]),
     "vp_forward_z0": (_I, [_P, _I64, _I64, _I64, _P, _I64, _I64, _I64, _P, _I64, _I, _P]),

@@ -12,10 +12,13 @@
 //     [0, PX) read as zero, which is what the border-mode texture returned;
 //   * all angles accumulate in registers and each voxel is updated with a
 //     single read-modify-write at the end, so no atomics are needed.
+#include <cuda.h>
 #include <cuda_runtime.h>
+#include <cudaTypedefs.h>
 
 #include "vp_bp_block.cuh"
 #include "vp_bp_runs.cuh"
+#include "vp_bp_runs_tma.cuh"
 #include "vp_common.cuh"
 #include "vp_launch.h"
 
@@ -154,22 +157,86 @@ __global__ void __launch_bounds__(32 * BPB_WARPS)
 // saw no angle of its class leaves x untouched (in store mode the first launch
 // always writes).
 // ---------------------------------------------------------------------------
+// Origin of run `run` of class PASS.  Class 1 runs go along y (RUN rows) and
+// are numbered along x, so the warps of a block take neighbouring columns.
+// Class 0 runs go along x; they are numbered in bands of RUN rows, x-run
+// major, so the warps of a block take the same x-run in RUN neighbouring
+// rows.  Either way the four warps' windows at one angle are a fraction of a
+// bin apart and mostly shared through L1.
+template <int PASS>
+__device__ __forceinline__ void run_origin(int run, int nrun_major, int* xi0, int* yi0) {
+  if (PASS == 0) {
+    const int band = run / (RUN * nrun_major);
+    const int q = run - band * RUN * nrun_major;
+    *xi0 = (q / RUN) * RUN;
+    *yi0 = band * RUN + q % RUN;
+  } else {
+    *xi0 = run % nrun_major;
+    *yi0 = (run / nrun_major) * RUN;
+  }
+}
+
 template <int PASS, int R>
 __global__ void __launch_bounds__(32 * BPR_WARPS, R == 8 ? 5 : 0)
     bp_z0_runs_kernel(const float* __restrict__ y, float* __restrict__ x,
                       const float* __restrict__ angles, Geom g, int nrun_major, int run_base,
-                      int run_end, int accumulate) {
+                      int run_end, int row_end, int accumulate) {
   __shared__ RunEntry tab[BPR_WARPS][BPR_CHUNK];
   __shared__ int alist[BPR_WARPS][BPR_LIST];
   const int lane = threadIdx.x;
   const int w = threadIdx.y;
   const int run = run_base + blockIdx.x * BPR_WARPS + w;
   if (run >= run_end) return;  // warp-uniform; all shared state is per warp
-  // PASS 0: run along x starting at (xi0, yi0); PASS 1: along y.
-  const int xi0 = PASS == 0 ? (run % nrun_major) * RUN : run % nrun_major;
-  const int yi0 = PASS == 0 ? run / nrun_major : (run / nrun_major) * RUN;
+  int xi0, yi0;
+  run_origin<PASS>(run, nrun_major, &xi0, &yi0);
+  if (yi0 >= row_end) return;
   bp_runs_warp<PASS, R>(y, x, angles, g, xi0, yi0, blockIdx.y * 32 * R + lane * 4, accumulate,
                         tab[w], alist[w]);
+}
+
+// Bounded-wait timeouts of this library's kernels (0 in correct operation).
+__device__ unsigned long long g_wait_timeouts = 0;
+
+// The run adjoint with 8 heights per lane and each angle's bin window staged
+// once per block by bulk copies (vp_bp_runs_tma.cuh): 4 compute warps on a
+// 4 x 4 voxel tile (run_origin) and a copy warp.  Blocks that cannot stage (a
+// partial height chunk, runs past the range) run bp_runs_warp instead.
+constexpr size_t kTmaBlockSmem = sizeof(TmaBlockSmem);
+
+template <int PASS>
+__global__ void __launch_bounds__(TMA_THREADS, 4)
+    bp_z0_runs_tma_kernel(const float* __restrict__ y, float* __restrict__ x,
+                          const float* __restrict__ angles, Geom g, int nrun_major,
+                          int run_base, int run_end, int row_end, int accumulate,
+                          const __grid_constant__ CUtensorMap ymap) {
+  extern __shared__ __align__(128) unsigned char tma_smem[];
+  TmaBlockSmem& sm = *reinterpret_cast<TmaBlockSmem*>(tma_smem);
+  const int lane = threadIdx.x & 31;
+  const int w = threadIdx.x >> 5;
+  const int h0 = blockIdx.y * 32 * 8;
+  // block-uniform: can every compute warp's run be staged?
+  const int first = run_base + blockIdx.x * TMA_WARPS;
+  bool staged = h0 + 32 * 8 <= g.H && first + TMA_WARPS <= run_end;
+  if (staged) {
+    int xo, yo;
+    run_origin<PASS>(first + TMA_WARPS - 1, nrun_major, &xo, &yo);
+    staged = yo < row_end;
+    run_origin<PASS>(first, nrun_major, &xo, &yo);
+    staged = staged && yo < row_end;
+  }
+  const int run = first + (w < TMA_WARPS ? w : 0);
+  int xi0, yi0;
+  run_origin<PASS>(run, nrun_major, &xi0, &yi0);
+  if (staged) {
+    bp_runs_tma_block<PASS>(y, x, angles, g, xi0, yi0, h0, accumulate, sm, &ymap,
+                            &g_wait_timeouts);
+    return;
+  }
+  if (w >= TMA_WARPS || run >= run_end || yi0 >= row_end) return;
+  RunEntry* tab = reinterpret_cast<RunEntry*>(&sm.ring[0][0]) + w * BPR_CHUNK;
+  int* alist = reinterpret_cast<int*>(reinterpret_cast<RunEntry*>(&sm.ring[0][0]) +
+                                      TMA_WARPS * BPR_CHUNK) + w * BPR_LIST;
+  bp_runs_warp<PASS, 8>(y, x, angles, g, xi0, yi0, h0 + lane * 4, accumulate, tab, alist);
 }
 
 // ---------------------------------------------------------------------------
@@ -275,6 +342,76 @@ cudaError_t launch_bp_z0_block(const float* y, float* x, const float* angles, co
   return cudaGetLastError();
 }
 
+// The sinogram as a 3-D tensor (heights, bins, angles) with boxes of 256
+// heights x TMA_NBMAX bins x 1 angle, for the staged adjoint.
+cudaError_t sinogram_tensor_map(const float* y, const Geom& g, CUtensorMap* map) {
+  static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+  if (encode == nullptr) {
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    const cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000,
+                                                           cudaEnableDefault, &q);
+    if (e != cudaSuccess) return e;
+    if (q != cudaDriverEntryPointSuccess || fn == nullptr) return cudaErrorNotSupported;
+    encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+  }
+  const cuuint64_t dims[3] = {(cuuint64_t)g.Hy, (cuuint64_t)g.PX, (cuuint64_t)g.n_ang};
+  const cuuint64_t strides[2] = {(cuuint64_t)g.Hy * sizeof(float),
+                                 (cuuint64_t)g.PX * g.Hy * sizeof(float)};
+  const cuuint32_t box[3] = {(cuuint32_t)TMA_BIN_FLOATS, (cuuint32_t)TMA_NBMAX, 1};
+  const cuuint32_t estride[3] = {1, 1, 1};
+  const CUresult r = encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float*>(y), dims,
+                            strides, box, estride, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                            CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
+}
+
+cudaError_t launch_bp_z0_runs_tma(const float* y, float* x, const float* angles, const Geom& g,
+                                  int row_lo, int row_hi, cudaStream_t stream) {
+  CUtensorMap ymap;
+  cudaError_t e0m = sinogram_tensor_map(y, g, &ymap);
+  if (e0m != cudaSuccess) return e0m;
+  static bool configured[64] = {};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev >= 0 && dev < 64 && !configured[dev]) {
+    // the attribute is per device; setting it twice is harmless
+    for (const void* k : {reinterpret_cast<const void*>(bp_z0_runs_tma_kernel<0>),
+                          reinterpret_cast<const void*>(bp_z0_runs_tma_kernel<1>)}) {
+      e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)kTmaBlockSmem);
+      if (e == cudaSuccess)  // room for four blocks per SM
+        e = cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+      if (e != cudaSuccess) return e;
+    }
+    configured[dev] = true;
+  }
+  dim3 block(TMA_THREADS);
+  const unsigned hchunks = ceil_div(g.H, 32 * 8);
+  const int nmaj0 = (int)ceil_div(g.SX, RUN);
+  // class-0 runs in bands of RUN rows (run_origin): row_lo is a multiple of RUN
+  const long long b0 = (long long)row_lo * nmaj0;
+  const long long e0 = (long long)ceil_div(row_hi, RUN) * RUN * nmaj0;
+  if (e0 > b0) {
+    bp_z0_runs_tma_kernel<0><<<dim3(ceil_div(e0 - b0, TMA_WARPS), hchunks), block,
+                               kTmaBlockSmem, stream>>>(y, x, angles, g, nmaj0, (int)b0,
+                                                        (int)e0, row_hi, g.accumulate, ymap);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  const long long b1 = (long long)(row_lo / RUN) * g.SX;
+  const long long e1 = (long long)ceil_div(row_hi, RUN) * g.SX;
+  if (e1 > b1) {
+    bp_z0_runs_tma_kernel<1><<<dim3(ceil_div(e1 - b1, TMA_WARPS), hchunks), block,
+                               kTmaBlockSmem, stream>>>(y, x, angles, g, g.SX, (int)b1,
+                                                        (int)e1, row_hi, 1, ymap);
+    return cudaGetLastError();
+  }
+  return cudaSuccess;
+}
+
 // Both class launches for the voxel rows [row_lo, row_hi); row_lo is a
 // multiple of RUN (class-1 runs span RUN rows).
 template <int R>
@@ -283,10 +420,12 @@ cudaError_t launch_bp_z0_runs(const float* y, float* x, const float* angles, con
   dim3 block(32, BPR_WARPS);
   const unsigned hchunks = ceil_div(g.H, 32 * R);
   const int nmaj0 = (int)ceil_div(g.SX, RUN);
-  const long long b0 = (long long)row_lo * nmaj0, e0 = (long long)row_hi * nmaj0;
+  // class-0 runs in bands of RUN rows (run_origin): row_lo is a multiple of RUN
+  const long long b0 = (long long)row_lo * nmaj0;
+  const long long e0 = (long long)ceil_div(row_hi, RUN) * RUN * nmaj0;
   if (e0 > b0) {
     bp_z0_runs_kernel<0, R><<<dim3(ceil_div(e0 - b0, BPR_WARPS), hchunks), block, 0, stream>>>(
-        y, x, angles, g, nmaj0, (int)b0, (int)e0, g.accumulate);
+        y, x, angles, g, nmaj0, (int)b0, (int)e0, row_hi, g.accumulate);
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
   }
@@ -294,7 +433,7 @@ cudaError_t launch_bp_z0_runs(const float* y, float* x, const float* angles, con
   const long long e1 = (long long)ceil_div(row_hi, RUN) * g.SX;
   if (e1 > b1) {
     bp_z0_runs_kernel<1, R><<<dim3(ceil_div(e1 - b1, BPR_WARPS), hchunks), block, 0, stream>>>(
-        y, x, angles, g, g.SX, (int)b1, (int)e1, 1);
+        y, x, angles, g, g.SX, (int)b1, (int)e1, row_hi, 1);
     return cudaGetLastError();
   }
   return cudaSuccess;
@@ -306,12 +445,14 @@ int bp0_split(const Geom& g) { return g.H > 128 ? r8_heights(g.H) : 0; }
 
 cudaError_t launch_bp_z0_runs_split(const float* y, float* x, const float* angles,
                                     const Geom& g, int row_lo, int row_hi,
-                                    cudaStream_t stream) {
+                                    cudaStream_t stream, bool tma = false) {
   const int H8 = bp0_split(g);
   if (H8 > 0) {
     Geom g8 = g;
     g8.H = H8;
-    const cudaError_t e = launch_bp_z0_runs<8>(y, x, angles, g8, row_lo, row_hi, stream);
+    const cudaError_t e =
+        tma ? launch_bp_z0_runs_tma(y, x, angles, g8, row_lo, row_hi, stream)
+            : launch_bp_z0_runs<8>(y, x, angles, g8, row_lo, row_hi, stream);
     if (e != cudaSuccess || H8 == g.H) return e;
   }
   Geom g4 = g;
@@ -337,8 +478,8 @@ int launches_backward_z0(const float* y, const float* x, const Geom& g) {
 // axis of smaller step, two launches (bp_z0_runs_kernel); 7 = runs with 8
 // heights per lane (two float4, 128 heights apart; problems of at most 128
 // heights run 6, and a last chunk of at most 128 heights runs with 4 per
-// lane).  The default when heights come in float4 is 7, the fastest at 512^3
-// with 192 angles.
+// lane); 9 = as 7 with each angle's windows staged per block by bulk copies
+// (bp_z0_runs_tma_kernel).  The default when heights come in float4 is 7.
 cudaError_t launch_backward_z0(const float* y, float* x, const float* angles, const Geom& g,
                                cudaStream_t stream) {
   const bool vec4 = bp0_vec4(y, x, g);
@@ -350,6 +491,7 @@ cudaError_t launch_backward_z0(const float* y, float* x, const float* angles, co
       case 4: return launch_bp_z0_block<2, 2>(y, x, angles, g, stream);
       case 5: return launch_bp_z0_block<8, 2>(y, x, angles, g, stream);
       case 6: return launch_bp_z0_runs<4>(y, x, angles, g, 0, g.SY, stream);
+      case 9: return launch_bp_z0_runs_split(y, x, angles, g, 0, g.SY, stream, true);
       default: return launch_bp_z0_runs_split(y, x, angles, g, 0, g.SY, stream);
     }
   }
@@ -363,6 +505,12 @@ cudaError_t launch_backward_z0(const float* y, float* x, const float* angles, co
   return cudaGetLastError();
 }
 
+unsigned long long wait_timeouts() {
+  unsigned long long n = 0;
+  if (cudaMemcpyFromSymbol(&n, g_wait_timeouts, sizeof(n)) != cudaSuccess) return ~0ull;
+  return n;
+}
+
 int backward_z0_row_step(const float* y, const float* x, const Geom& g) {
   const int v = kernel_variant(OP_BACKWARD_Z0);
   return (bp0_vec4(y, x, g) && (v < 1 || v > 5)) ? RUN : 0;
@@ -373,9 +521,9 @@ cudaError_t launch_backward_z0_rows(const float* y, float* x, const float* angle
                                     cudaStream_t stream) {
   if (row_lo == 0 && row_hi == g.SY) return launch_backward_z0(y, x, angles, g, stream);
   if (backward_z0_row_step(y, x, g) == 0 || row_lo % RUN != 0) return cudaErrorInvalidValue;
-  if (kernel_variant(OP_BACKWARD_Z0) == 6)
-    return launch_bp_z0_runs<4>(y, x, angles, g, row_lo, row_hi, stream);
-  return launch_bp_z0_runs_split(y, x, angles, g, row_lo, row_hi, stream);
+  const int v = kernel_variant(OP_BACKWARD_Z0);
+  if (v == 6) return launch_bp_z0_runs<4>(y, x, angles, g, row_lo, row_hi, stream);
+  return launch_bp_z0_runs_split(y, x, angles, g, row_lo, row_hi, stream, v == 9);
 }
 
 cudaError_t launch_backward_z2(const float* y, float* x, const float* angles, const Geom& g,

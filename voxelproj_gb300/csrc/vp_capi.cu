@@ -188,6 +188,8 @@ int vp_last_cuda_error(void) { return g_last_cuda_error; }
 
 uint64_t vp_launch_count(void) { return g_launches.load(std::memory_order_relaxed); }
 
+uint64_t vp_wait_timeouts(void) { return vp::wait_timeouts(); }
+
 int vp_forward_z0(const float* x, int64_t x0, int64_t x1, int64_t x2, float* y, int64_t y0,
                   int64_t y1, int64_t y2, const float* angles, int64_t n_angles, int flags,
                   void* stream) {

@@ -80,6 +80,8 @@ cudaError_t launch_forward_z0_stream(const float* x, float* y, const float* angl
 cudaError_t launch_forward_z0_rest(const float* x, float* y, const float* angles,
                                    const Geom& g, cudaStream_t stream, int* launches);
 int backward_z0_row_step(const float* y, const float* x, const Geom& g);
+// Bounded waits in this library's kernels that ran out (synchronising read).
+unsigned long long wait_timeouts();
 cudaError_t launch_backward_z0_rows(const float* y, float* x, const float* angles,
                                     const Geom& g, int row_lo, int row_hi,
                                     cudaStream_t stream);

@@ -188,7 +188,8 @@ def test_backward_variants_store_mode_via_z2(variant, H):
 
 @pytest.mark.parametrize("variant", [1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12])
 @pytest.mark.parametrize("geom", [(23, 37, 132, 61, 50, "wide"), (9, 6, 8, 40, 11, "axes"),
-                                  (70, 64, 256, 96, 90, "rand"), (30, 21, 260, 33, 40, "rand")],
+                                  (70, 64, 256, 96, 90, "rand"), (30, 21, 260, 33, 40, "rand"),
+                                  (26, 31, 1024, 23, 36, "wide")],
                          ids=lambda g: "x".join(map(str, g[:5])) + g[5])
 def test_forward_variants(variant, geom):
     """Every kernel variant of the z_order 0 forward against the oracle:
@@ -214,7 +215,7 @@ def test_forward_variants(variant, geom):
 
 
 @pytest.mark.parametrize("variant", [1, 5, 7, 8, 9, 12])
-@pytest.mark.parametrize("H", [36, 260])
+@pytest.mark.parametrize("H", [36, 260, 512])
 def test_forward_variants_store_mode_via_z2(variant, H):
     """The forward's first slab launch writes the z_order 2 scratch in store
     mode; repeated calls must not depend on the scratch's prior content."""

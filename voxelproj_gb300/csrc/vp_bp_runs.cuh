@@ -188,7 +188,7 @@ __device__ __forceinline__ void bp_runs_warp(const float* __restrict__ y, float*
   }
 
   wait();
-  if (lh.v0 && (seen > 0 || !accumulate)) {  // a lane past H has no second half either
+  if (lh.v[0] && (seen > 0 || !accumulate)) {  // a lane past H has no second half either
 #pragma unroll
     for (int m = 0; m < RUN; ++m) {
       const int xi = xi0 + m * dx;

@@ -344,7 +344,7 @@ __device__ __forceinline__ void bp_runs_tma_block(const float* __restrict__ y,
     }
     return;
   }
-  if (lh.v0 && (seen > 0 || !accumulate)) {
+  if (lh.v[0] && (seen > 0 || !accumulate)) {
 #pragma unroll
     for (int m = 0; m < RUN; ++m) {
       const int xi = xi0 + m * dx;

@@ -212,25 +212,29 @@ struct Vec<8> {
   using T = float4x2;
 };
 
-// Height offsets of one lane: R = 1 or 4 heights from h; R = 8 as float4x2
-// from h.  Lanes past H read offset 0 (always valid) and never store.
+// Height offsets of one lane: R = 1 or 4 heights from h; R = 8 as float4 at
+// h and h + 128.  Lanes past H read offset 0 (always valid) and never store.
 template <int R>
 struct LaneH {
-  int h, s0, d1;  // first height; load offset of the first half, second minus first
-  bool v0, v1;    // halves inside [0, H)
+  static constexpr int NQ = R == 8 ? 2 : 1;  // float4 per lane
+  int h, s0;
+  int d[NQ];   // load offset of float4 k minus s0
+  bool v[NQ];  // float4 k inside [0, H)
   __device__ __forceinline__ LaneH(int h_, int H) : h(h_) {
-    v0 = h < H;
-    s0 = v0 ? h : 0;
-    v1 = R == 8 && h + kSecondHalf < H;
-    d1 = (v1 ? h + kSecondHalf : 0) - s0;
+    s0 = h < H ? h : 0;
+#pragma unroll
+    for (int k = 0; k < NQ; ++k) {
+      v[k] = h + k * kSecondHalf < H;
+      d[k] = (v[k] ? h + k * kSecondHalf : 0) - s0;
+    }
   }
   // this lane's heights of a row, given q = row + s0
   __device__ __forceinline__ typename Vec<R>::T load(const float* q) const {
     if constexpr (R == 8) {
-      float4x2 v;
-      v.a = __ldg(reinterpret_cast<const float4*>(q));
-      v.b = __ldg(reinterpret_cast<const float4*>(q + d1));
-      return v;
+      float4x2 r;
+      r.a = __ldg(reinterpret_cast<const float4*>(q));
+      r.b = __ldg(reinterpret_cast<const float4*>(q + d[1]));
+      return r;
     } else {
       return __ldg(reinterpret_cast<const typename Vec<R>::T*>(q));
     }
@@ -277,15 +281,16 @@ template <int R, bool COHERENT = false>
 __device__ __forceinline__ void store_lane(float* p, const LaneH<R>& lh,
                                            const typename Vec<R>::T& v, int accumulate) {
   if constexpr (R == 8) {
-    if (lh.v0) {
-      float4* q = reinterpret_cast<float4*>(p + lh.h);
-      if constexpr (COHERENT) store_out_coherent(q, v.a); else store_out(q, v.a, accumulate);
+    const float4* parts = reinterpret_cast<const float4*>(&v);
+#pragma unroll
+    for (int k = 0; k < LaneH<R>::NQ; ++k) {
+      if (lh.v[k]) {
+        float4* q = reinterpret_cast<float4*>(p + lh.h + k * kSecondHalf);
+        if constexpr (COHERENT) store_out_coherent(q, parts[k]);
+        else store_out(q, parts[k], accumulate);
+      }
     }
-    if (lh.v1) {
-      float4* q = reinterpret_cast<float4*>(p + lh.h + kSecondHalf);
-      if constexpr (COHERENT) store_out_coherent(q, v.b); else store_out(q, v.b, accumulate);
-    }
-  } else if (lh.v0) {
+  } else if (lh.v[0]) {
     auto* q = reinterpret_cast<typename Vec<R>::T*>(p + lh.h);
     if constexpr (COHERENT && R == 4) store_out_coherent(q, v); else store_out(q, v, accumulate);
   }

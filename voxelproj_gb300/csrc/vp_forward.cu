@@ -132,8 +132,9 @@ struct Fp0Config {
 // heights per lane, 2 candidates in flight; 6 = as 5 with 4 in flight;
 // 7 = as 5 with 64 MB slabs; 8 = 8 bins, 8 heights per lane; 9 / 10 / 11 =
 // as 5 with class slabs of 32 / 64 / 128 MB (10 is the default); 12 = as 1
-// with class slabs of 32 MB.  Heights not in float4 run the scalar form of the same bin layout;
-// 8-height variants on problems of at most 128 heights run the 4-height form.
+// with class slabs of 32 MB.  Heights not in float4 run the scalar form of
+// the same bin layout; 8-height variants on problems of at most 128 heights
+// run the 4-height form.
 Fp0Config fp0_config(const Geom& g, bool vec4, int variant) {
   Fp0Config c{vec4 ? 4 : 1, 4, false, FP0_UNROLL, 32, false};
   if (variant == 0) variant = 10;  // the default (fastest at 512^3 with 192 angles)

@@ -54,14 +54,17 @@ def test_host_entries_match_oracle_and_device_path(geom, pinned):
     assert rel_err(xo.numpy() - x0.numpy(), oracle.backward(y.numpy(), ang, SY, SX, 0)) <= \
         tol.ref_vs_fp64(n_ext)
 
-    # the device entry points: same operator, summed in another order
+    # the device entry points: same operator, summed in another order (the
+    # host path's row and column pieces group the slab partial sums
+    # differently from the device path's class slabs; a few ulp of the
+    # largest output)
     yd = y0.cuda()
     vp._CU.forward_z0(x.cuda(), yd, a_host.cuda())
     xd = x0.cuda()
     vp._CU.backward_z0(y.cuda(), xd, a_host.cuda())
     torch.cuda.synchronize()
-    assert rel_err(yo.numpy(), yd.cpu().numpy()) <= 1e-6
-    assert rel_err(xo.numpy(), xd.cpu().numpy()) <= 1e-6
+    assert rel_err(yo.numpy(), yd.cpu().numpy()) <= 4e-6
+    assert rel_err(xo.numpy(), xd.cpu().numpy()) <= 4e-6
 
 
 @pytest.mark.parametrize("geom", GEOMS[1:], ids=lambda g: "x".join(map(str, g)))

@@ -131,13 +131,15 @@ struct Fp0Config {
 // neighbouring angles; 4 = 8 bins, neighbouring angles; 5 = 4 bins, 8
 // heights per lane, 2 candidates in flight; 6 = as 5 with 4 in flight;
 // 7 = as 5 with 64 MB slabs; 8 = 8 bins, 8 heights per lane; 9 / 10 / 11 =
-// as 5 with class slabs of 32 / 64 / 128 MB (10 is the default); 12 = as 1
+// as 5 with class slabs of 32 / 64 / 128 MB (10 is the default: 11 runs 1%
+// faster at 512^3 with 192 angles but misses L2 on the volume, 5.3 against
+// 4.6 GB of DRAM traffic per call); 12 = as 1
 // with class slabs of 32 MB.  Heights not in float4 run the scalar form of
 // the same bin layout; 8-height variants on problems of at most 128 heights
 // run the 4-height form.
 Fp0Config fp0_config(const Geom& g, bool vec4, int variant) {
   Fp0Config c{vec4 ? 4 : 1, 4, false, FP0_UNROLL, 32, false};
-  if (variant == 0) variant = 10;  // the default (fastest at 512^3 with 192 angles)
+  if (variant == 0) variant = 10;  // the default
   switch (variant) {
     case 2: c.KW = 8; break;
     case 3: c.agroup = true; break;
@@ -350,12 +352,17 @@ int launches_forward_z0(const float* x, const float* y, const Geom& g) {
 // the class slabs of the device path, spread over time.  The 4-height
 // remainder of a split heights range runs whole at the end
 // (launch_forward_z0_rest).
+// Pieces of at most 64 MB of one height chunk: pieces are copy and overlap
+// units as well as slabs, and smaller ones start the kernels sooner.
+constexpr int kStreamPieceMB = 64;
+
 int forward_z0_stream_rows(const float* x, const float* y, const Geom& g) {
   const bool vec4 = fp0_vec4(x, y, g);
   const int v = kernel_variant(OP_FORWARD_Z0);
   const Geom gm = fp0_parts(g, vec4, v).g[0];
   Fp0Config c = fp0_config(gm, vec4, v);
   c.cls = false;  // rows of one class alone: the row-slab budget
+  c.slab_mb = c.slab_mb < kStreamPieceMB ? c.slab_mb : kStreamPieceMB;
   return fp0_slab_rows(gm, c);
 }
 
@@ -365,6 +372,7 @@ int forward_z0_stream_cols(const float* x, const float* y, const Geom& g) {
   const Geom gm = fp0_parts(g, vec4, v).g[0];
   Fp0Config c = fp0_config(gm, vec4, v);
   c.cls = false;
+  c.slab_mb = c.slab_mb < kStreamPieceMB ? c.slab_mb : kStreamPieceMB;
   Geom gt = gm;  // columns of the other class: rows and columns swapped
   gt.SY = gm.SX;
   gt.SX = gm.SY;

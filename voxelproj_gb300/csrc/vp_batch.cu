@@ -149,11 +149,11 @@ __device__ __forceinline__ void run_bwd_runs_item(const BatchDesc& d, int stage,
   const int run = grp * BATCH_WARPS + w;
   const int h = hc * 32 * R + lane * 4;
   if (stage == 0) {
-    if (run < d.nruns0) {
-      const int nmaj = (d.g.SX + RUN - 1) / RUN;
-      bp_runs_warp<0, R>(d.in, d.out, d.angles, d.g, (run % nmaj) * RUN, run / nmaj, h, 1,
-                         sm.runs.tab[w], sm.runs.alist[w]);
-    }
+    int xi0, yi0;
+    run_origin<0>(run, (d.g.SX + RUN - 1) / RUN, &xi0, &yi0);
+    if (run < d.nruns0 && yi0 < d.g.SY)
+      bp_runs_warp<0, R>(d.in, d.out, d.angles, d.g, xi0, yi0, h, 1, sm.runs.tab[w],
+                         sm.runs.alist[w]);
   } else if (run < d.nruns1) {
     const StageWait wt{ctr - 1, (unsigned)(d.groups0 * BATCH_WARPS), error};
     bp_runs_warp<1, R>(d.in, d.out, d.angles, d.g, run % d.g.SX, (run / d.g.SX) * RUN, h, 1,
@@ -285,7 +285,9 @@ int part_desc(const vp_batch_problem& p, const vp::Geom& g, const float* in, flo
     d->kind = vp::K_BWD_RUNS;
     d->R = R;
     d->nstages = 2;
-    d->nruns0 = (int)vp::ceil_div_u(g.SX, vp::detail::RUN) * g.SY;
+    // class-0 runs in bands of RUN rows (run_origin), rows padded to the band
+    d->nruns0 = (int)vp::ceil_div_u(g.SX, vp::detail::RUN) *
+                (int)vp::ceil_div_u(g.SY, vp::detail::RUN) * vp::detail::RUN;
     d->nruns1 = g.SX * (int)vp::ceil_div_u(g.SY, vp::detail::RUN);
     d->groups0 = (int)vp::ceil_div_u(d->nruns0, vp::BATCH_WARPS);
     d->groups1 = (int)vp::ceil_div_u(d->nruns1, vp::BATCH_WARPS);

@@ -47,6 +47,25 @@ __device__ __forceinline__ void run_window(typename Vec<R>::T (&acc)[RUN], const
   }
 }
 
+// Origin of run `run` of class PASS.  Class 1 runs go along y (RUN rows) and
+// are numbered along x, so the warps of a block take neighbouring columns.
+// Class 0 runs go along x; they are numbered in bands of RUN rows, x-run
+// major, so the warps of a block take the same x-run in RUN neighbouring
+// rows.  Either way the four warps' windows at one angle are a fraction of a
+// bin apart and mostly shared through L1.
+template <int PASS>
+__device__ __forceinline__ void run_origin(int run, int nrun_major, int* xi0, int* yi0) {
+  if (PASS == 0) {
+    const int band = run / (RUN * nrun_major);
+    const int q = run - band * RUN * nrun_major;
+    *xi0 = (q / RUN) * RUN;
+    *yi0 = band * RUN + q % RUN;
+  } else {
+    *xi0 = run % nrun_major;
+    *yi0 = (run / nrun_major) * RUN;
+  }
+}
+
 template <int PASS>
 __device__ __forceinline__ bool in_class(float phi, int trig) {
   float s, c;

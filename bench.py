@@ -77,6 +77,22 @@ def dist_info():
     return world, rank, local
 
 
+def max_over_ranks(value: float, world: int, device) -> float:
+    """The largest per-rank value over all ranks: a job's time is its slowest
+    rank's.  Needs the default process group when world > 1."""
+    if world <= 1:
+        return float(value)
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_gvu_s(world: int, steps: int, vu_step: float, total_ms: float) -> float:
+    """Voxel-angle updates of all ranks / the slowest rank's time, in GVU/s.
+    Replicas: every rank runs its own problem of vu_step updates per step."""
+    return world * steps * vu_step / (total_ms / 1e3) / 1e9
+
+
 def shapes(S, n, z):
     xs = (S, S, S)
     ys = (n, S, S) if z == 0 else (S, n, S)
@@ -334,13 +350,9 @@ def run_ours(args, world, rank, local):
     total_ms = start.elapsed_time(end)
     t_fwd = [e[0].elapsed_time(e[1]) for e in evs]
     t_bwd = [e[1].elapsed_time(e[2]) for e in evs]
-    if world > 1:
-        tt = torch.tensor([total_ms], device=dev)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(tt.item())
-
+    total_ms = max_over_ranks(total_ms, world, dev)
     vu_step = 2 * S**3 * n
-    value = world * args.steps * vu_step / (total_ms / 1e3) / 1e9
+    value = whole_job_gvu_s(world, args.steps, vu_step, total_ms)
     fwd_ms = statistics.mean(t_fwd)
     bwd_ms = statistics.mean(t_bwd)
 

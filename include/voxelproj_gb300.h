@@ -214,7 +214,7 @@ VP_API int vp_batch_error(vp_batch_plan* plan, int* error);
 VP_API int vp_batch_destroy(vp_batch_plan* plan);
 
 /* ---- Host buffers --------------------------------------------------------
- * y (+)= A x and x (+)= A^T y, z_order 0, with x and y in host memory (any
+ * y (+)= A x and x (+)= A^T y with x and y in host memory (any
  * memory cudaMemcpyDefault can address); angles in host or device memory.
  * Dims as for vp_forward_z0 / vp_backward_z0.  The library stages the arrays
  * through device buffers of its own pool and overlaps the copies with the
@@ -232,6 +232,16 @@ VP_API int vp_forward_z0_host(const float* x, int64_t x0, int64_t x1, int64_t x2
                               int64_t y0, int64_t y1, int64_t y2, const float* angles,
                               int64_t n_angles, int flags, void* stream);
 VP_API int vp_backward_z0_host(const float* y, int64_t y0, int64_t y1, int64_t y2, float* x,
+                               int64_t x0, int64_t x1, int64_t x2, const float* angles,
+                               int64_t n_angles, int flags, void* stream);
+/* The same for z_order 2, dims as for vp_forward_z2 / vp_backward_z2.  Heights
+ * are the slowest axis there, so the library works in chunks of heights (256
+ * from 512 heights up), each an independent problem whose copies overlap the
+ * other chunk's kernels. */
+VP_API int vp_forward_z2_host(const float* x, int64_t x0, int64_t x1, int64_t x2, float* y,
+                              int64_t y0, int64_t y1, int64_t y2, const float* angles,
+                              int64_t n_angles, int flags, void* stream);
+VP_API int vp_backward_z2_host(const float* y, int64_t y0, int64_t y1, int64_t y2, float* x,
                                int64_t x0, int64_t x1, int64_t x2, const float* angles,
                                int64_t n_angles, int flags, void* stream);
 

@@ -50,7 +50,8 @@ DUMMY = ctypes.c_void_p(0x1000)  # never dereferenced: validation fails first
 
 
 @pytest.mark.parametrize("fn", ["vp_forward_z0", "vp_backward_z0", "vp_forward_z2",
-                                "vp_backward_z2", "vp_forward_z0_host", "vp_backward_z0_host"])
+                                "vp_backward_z2", "vp_forward_z0_host", "vp_backward_z0_host",
+                                "vp_forward_z2_host", "vp_backward_z2_host"])
 def test_validation_errors_without_gpu(fn):
     f = getattr(_lib.LIB, fn)
     good = (4, 5, 6)

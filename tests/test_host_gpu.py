@@ -140,3 +140,55 @@ def test_host_path_repeated_calls_reuse_pool():
         _call("vp_forward_z0_host", x, yo, ang)
         outs.append(yo.clone())
     assert torch.equal(outs[0], outs[1]) and torch.equal(outs[1], outs[2])
+
+
+# z_order 2 (H, SY, SX): one chunk with the small-height kernels, two chunks
+# through the transposed path, and chunks of 256 heights with a ragged last one
+Z2_GEOMS = [(20, 24, 12, 30, 28), (33, 29, 100, 21, 40), (28, 26, 600, 17, 30)]
+
+
+@pytest.mark.parametrize("geom", Z2_GEOMS, ids=lambda g: "x".join(map(str, g)))
+def test_z2_host_entries(geom):
+    SY, SX, H, n, PX = geom
+    ang = lin(n, -0.2, 3.3)
+    x = torch.tensor(seeded((H, SY, SX), 21)).pin_memory()
+    y = torch.tensor(seeded((H, n, PX), 22)).pin_memory()
+    y0 = torch.tensor(seeded((H, n, PX), 23)).pin_memory()
+    x0 = torch.tensor(seeded((H, SY, SX), 24))
+    a = torch.tensor(ang)
+    yo = y0.clone()
+    _call("vp_forward_z2_host", x, yo, a)
+    xo = x0.clone()
+    _call("vp_backward_z2_host", y, xo, a)
+    n_ext = max(SY, SX, PX)
+    assert rel_err(yo.numpy() - y0.numpy(), oracle.forward(x.numpy(), ang, PX, 2)) <= \
+        tol.ref_vs_fp64(n_ext)
+    assert rel_err(xo.numpy() - x0.numpy(), oracle.backward(y.numpy(), ang, SY, SX, 2)) <= \
+        tol.ref_vs_fp64(n_ext)
+    # the device z_order 2 path per chunk is the same arithmetic: equal
+    yd = y0.cuda()
+    vp._CU.forward_z2(x.cuda(), yd, a.cuda())
+    xd = x0.cuda()
+    vp._CU.backward_z2(y.cuda(), xd, a.cuda())
+    torch.cuda.synchronize()
+    assert rel_err(yo.numpy(), yd.cpu().numpy()) <= 4e-6
+    assert rel_err(xo.numpy(), xd.cpu().numpy()) <= 4e-6
+    # out = result, heights past the input's extent zeroed
+    yw = torch.full((H + 8, n, PX), 3.0)
+    _call("vp_forward_z2_host", x, yw, a, _lib.VP_FLAG_OVERWRITE)
+    assert rel_err(yw.numpy()[:H], oracle.forward(x.numpy(), ang, PX, 2)) <= \
+        tol.ref_vs_fp64(n_ext)
+    assert not yw[H:].any()
+
+
+def test_wrappers_take_the_host_path_for_z2():
+    SY, SX, H, n = 30, 30, 40, 25
+    ang = lin(n)
+    x = seeded((H, SY, SX), 25)
+    before = _lib.LIB.vp_launch_count()
+    y = vp.forward(x, ang, None, z_order=2)
+    assert isinstance(y, np.ndarray) and y.shape == (H, n, 30)
+    assert rel_err(y, oracle.forward(x, ang, 30, 2)) <= tol.REF_VS_FP64
+    xb = vp.backward(y, ang, None, z_order=2)
+    assert rel_err(xb, oracle.backward(y, ang, 30, 30, 2)) <= tol.REF_VS_FP64
+    assert _lib.LIB.vp_launch_count() > before

@@ -77,6 +77,8 @@ SIGNATURES = {
     "vp_batch_destroy": (_I, [_P]),
     "vp_forward_z0_host": (_I, [_P, _I64, _I64, _I64, _P, _I64, _I64, _I64, _P, _I64, _I, _P]),
     "vp_backward_z0_host": (_I, [_P, _I64, _I64, _I64, _P, _I64, _I64, _I64, _P, _I64, _I, _P]),
+    "vp_forward_z2_host": (_I, [_P, _I64, _I64, _I64, _P, _I64, _I64, _I64, _P, _I64, _I, _P]),
+    "vp_backward_z2_host": (_I, [_P, _I64, _I64, _I64, _P, _I64, _I64, _I64, _P, _I64, _I, _P]),
     "vp_forward": (_I, [_P, _P, _P, _P, _P, _I64, _I, _I, _P]),
     "vp_backward": (_I, [_P, _P, _P, _P, _P, _I64, _I, _I, _P]),
 }

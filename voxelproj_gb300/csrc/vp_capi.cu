@@ -129,15 +129,18 @@ cudaError_t zero_any(float* out, int64_t n, cudaStream_t s) {
   return e != cudaSuccess ? e : f;
 }
 
+// x and y dims in the caller's order; z2: heights first (x (Hx, SY, SX),
+// y (Hy, n_ang, PX)), else last.
 template <class Run>
-int host_entry(const float* x, int64_t x0, int64_t x1, int64_t x2, const float* y, int64_t y0,
-               int64_t y1, int64_t y2, float* out, int64_t out_elems, const float* angles,
-               int64_t n_angles, int flags, void* stream, Run run) {
+int host_entry(bool z2, const float* x, int64_t x0, int64_t x1, int64_t x2, const float* y,
+               int64_t y0, int64_t y1, int64_t y2, float* out, int64_t out_elems,
+               const float* angles, int64_t n_angles, int flags, void* stream, Run run) {
   const bool overwrite = (flags & VP_FLAG_OVERWRITE) != 0;
   vp::Geom g;
   bool empty = false;
-  if (int s = make_geom(x, x0, x1, x2, y, y0, y1, y2, angles, n_angles,
-                        flags & ~VP_FLAG_OVERWRITE, &g, &empty))
+  const int f = flags & ~VP_FLAG_OVERWRITE;
+  if (int s = z2 ? make_geom(x, x1, x2, x0, y, y1, y2, y0, angles, n_angles, f, &g, &empty)
+                 : make_geom(x, x0, x1, x2, y, y0, y1, y2, angles, n_angles, f, &g, &empty))
     return s;
   const cudaStream_t st = (cudaStream_t)stream;
   if (empty) return overwrite ? finish(zero_any(out, out_elems, st), 0) : VP_OK;
@@ -217,8 +220,9 @@ int vp_backward_z0(const float* y, int64_t y0, int64_t y1, int64_t y2, float* x,
 int vp_forward_z0_host(const float* x, int64_t x0, int64_t x1, int64_t x2, float* y, int64_t y0,
                        int64_t y1, int64_t y2, const float* angles, int64_t n_angles, int flags,
                        void* stream) {
-  return host_entry(x, x0, x1, x2, y, y0, y1, y2, y, y0 * y1 * y2, angles, n_angles, flags,
-                    stream, [&](const vp::Geom& g, cudaMemPool_t pool, cudaStream_t s, int* n) {
+  return host_entry(false, x, x0, x1, x2, y, y0, y1, y2, y, y0 * y1 * y2, angles, n_angles,
+                    flags, stream,
+                    [&](const vp::Geom& g, cudaMemPool_t pool, cudaStream_t s, int* n) {
                       return vp::forward_z0_host(x, y, angles, g, pool, s, n);
                     });
 }
@@ -226,9 +230,30 @@ int vp_forward_z0_host(const float* x, int64_t x0, int64_t x1, int64_t x2, float
 int vp_backward_z0_host(const float* y, int64_t y0, int64_t y1, int64_t y2, float* x, int64_t x0,
                         int64_t x1, int64_t x2, const float* angles, int64_t n_angles, int flags,
                         void* stream) {
-  return host_entry(x, x0, x1, x2, y, y0, y1, y2, x, x0 * x1 * x2, angles, n_angles, flags,
-                    stream, [&](const vp::Geom& g, cudaMemPool_t pool, cudaStream_t s, int* n) {
+  return host_entry(false, x, x0, x1, x2, y, y0, y1, y2, x, x0 * x1 * x2, angles, n_angles,
+                    flags, stream,
+                    [&](const vp::Geom& g, cudaMemPool_t pool, cudaStream_t s, int* n) {
                       return vp::backward_z0_host(y, x, angles, g, pool, s, n);
+                    });
+}
+
+int vp_forward_z2_host(const float* x, int64_t x0, int64_t x1, int64_t x2, float* y, int64_t y0,
+                       int64_t y1, int64_t y2, const float* angles, int64_t n_angles, int flags,
+                       void* stream) {
+  return host_entry(true, x, x0, x1, x2, y, y0, y1, y2, y, y0 * y1 * y2, angles, n_angles,
+                    flags, stream,
+                    [&](const vp::Geom& g, cudaMemPool_t pool, cudaStream_t s, int* n) {
+                      return vp::z2_host(true, x, y, angles, g, pool, s, n);
+                    });
+}
+
+int vp_backward_z2_host(const float* y, int64_t y0, int64_t y1, int64_t y2, float* x, int64_t x0,
+                        int64_t x1, int64_t x2, const float* angles, int64_t n_angles, int flags,
+                        void* stream) {
+  return host_entry(true, x, x0, x1, x2, y, y0, y1, y2, x, x0 * x1 * x2, angles, n_angles,
+                    flags, stream,
+                    [&](const vp::Geom& g, cudaMemPool_t pool, cudaStream_t s, int* n) {
+                      return vp::z2_host(false, y, x, angles, g, pool, s, n);
                     });
 }
 

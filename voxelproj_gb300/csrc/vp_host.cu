@@ -381,4 +381,84 @@ cudaError_t backward_z0_host(const float* y_host, float* x_host, const float* an
   }, s);
 }
 
+// z_order 2 with host arrays.  Heights are the slowest axis of both arrays,
+// so a chunk of heights is a contiguous, independent problem.  Chunks
+// alternate between two kernel streams; each chunk's copies in, projection
+// (the device z_order 2 path) and copy out run on its stream, so one chunk's
+// copies overlap the other chunk's kernels.  Chunks of 256 heights (the
+// 8-heights-per-lane kernels' chunk) from 512 heights up, else halves.
+cudaError_t z2_host(bool forward, const float* in_host, float* out_host, const float* angles,
+                    const Geom& g, cudaMemPool_t pool, cudaStream_t s, int* launches) {
+  std::lock_guard<std::mutex> lock(g_mutex);
+  const size_t vox = (size_t)g.SY * g.SX, bins = (size_t)g.n_ang * g.PX;
+  const size_t in_per_h = forward ? vox : bins;
+  const size_t out_per_h = forward ? bins : vox;
+  const int H = g.H;
+  const int Hout = forward ? g.Hy : g.Hx;
+  int Hc = H;
+  if (H >= 512) Hc = 256;
+  else if (H > 64) Hc = ((H + 1) / 2 + 3) / 4 * 4;
+  const int nchunks = (H + Hc - 1) / Hc;
+  Geom gc = g;  // a full chunk
+  gc.H = gc.Hx = gc.Hy = Hc;
+  Buffers buf(s);
+  return guarded([&]() -> cudaError_t {
+    float *in_d[2] = {}, *out_d[2] = {}, *ws[2] = {}, *as = nullptr;
+    const float* ad = nullptr;
+    const size_t ws_elems = z2_workspace_bytes(gc) / sizeof(float);
+    const int slots = nchunks > 1 ? 2 : 1;
+    for (int i = 0; i < slots; ++i) {
+      VP_TRY(buf.get(pool, (size_t)Hc * in_per_h * sizeof(float), &in_d[i]));
+      VP_TRY(buf.get(pool, (size_t)Hc * out_per_h * sizeof(float), &out_d[i]));
+      if (ws_elems > 0) VP_TRY(buf.get(pool, ws_elems * sizeof(float), &ws[i]));
+    }
+    VP_TRY(alloc_angles(angles, g, buf, pool, &ad, &as));
+    HostCtx* c = nullptr;
+    VP_TRY(get_ctx(2, &c));
+    cudaEvent_t ev_ready = c->ev[0], ev_c2 = c->ev[1];
+    VP_TRY(copy_angles(as, angles, g, s));
+    VP_TRY(cudaEventRecord(ev_ready, s));  // buffers allocated, angles in
+    VP_TRY(cudaStreamWaitEvent(c->compute2, ev_ready, 0));
+    const cudaStream_t st[2] = {s, c->compute2};
+    for (int k = 0; k < nchunks; ++k) {
+      const cudaStream_t t = st[k & 1];
+      float* in_k = in_d[k & 1];
+      float* out_k = out_d[k & 1];
+      const int h0 = k * Hc;
+      const int hc = h0 + Hc <= H ? Hc : H - h0;
+      Geom gk = g;
+      gk.H = gk.Hx = gk.Hy = hc;
+      gk.accumulate = 1;  // into the container's chunk, or zeros
+      VP_TRY(cudaMemcpyAsync(in_k, in_host + (size_t)h0 * in_per_h,
+                             (size_t)hc * in_per_h * sizeof(float), cudaMemcpyDefault, t));
+      if (g.accumulate)
+        VP_TRY(cudaMemcpyAsync(out_k, out_host + (size_t)h0 * out_per_h,
+                               (size_t)hc * out_per_h * sizeof(float), cudaMemcpyDefault, t));
+      else
+        VP_TRY(cudaMemsetAsync(out_k, 0, (size_t)hc * out_per_h * sizeof(float), t));
+      if (z2_uses_transpose(gk)) {
+        VP_TRY(forward ? forward_z2_transposed(in_k, out_k, ad, gk, ws[k & 1], t)
+                       : backward_z2_transposed(in_k, out_k, ad, gk, ws[k & 1], t));
+      } else {
+        VP_TRY(forward ? launch_forward_z2(in_k, out_k, ad, gk, t)
+                       : launch_backward_z2(in_k, out_k, ad, gk, t));
+      }
+      *launches += launches_z2(gk, forward);
+      VP_TRY(cudaMemcpyAsync(out_host + (size_t)h0 * out_per_h, out_k,
+                             (size_t)hc * out_per_h * sizeof(float), cudaMemcpyDefault, t));
+    }
+    if (!g.accumulate && Hout > H) {
+      // heights of the output past the input's extent: zero (out = result)
+      float* z = nullptr;
+      const size_t n = (size_t)(Hout - H) * out_per_h;
+      VP_TRY(buf.get(pool, n * sizeof(float), &z));
+      VP_TRY(cudaMemsetAsync(z, 0, n * sizeof(float), s));
+      VP_TRY(cudaMemcpyAsync(out_host + (size_t)H * out_per_h, z, n * sizeof(float),
+                             cudaMemcpyDefault, s));
+    }
+    VP_TRY(cudaEventRecord(ev_c2, c->compute2));
+    return cudaStreamWaitEvent(s, ev_c2, 0);  // s ends after both streams' chunks
+  }, s);
+}
+
 }  // namespace vp

@@ -92,6 +92,9 @@ cudaError_t forward_z0_host(const float* x_host, float* y_host, const float* ang
                             const Geom& g, cudaMemPool_t pool, cudaStream_t s, int* launches);
 cudaError_t backward_z0_host(const float* y_host, float* x_host, const float* angles,
                              const Geom& g, cudaMemPool_t pool, cudaStream_t s, int* launches);
+// z_order 2 (heights slowest): in is x for the forward, y for the adjoint.
+cudaError_t z2_host(bool forward, const float* in_host, float* out_host, const float* angles,
+                    const Geom& g, cudaMemPool_t pool, cudaStream_t s, int* launches);
 
 // Kernel launches the forward launchers issue for a geometry (grids are
 // split past 65535 angle blocks).

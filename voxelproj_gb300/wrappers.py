@@ -21,11 +21,11 @@ Beyond the reference: ``angles`` may also be a list or tuple (the reference
 accepted only arrays/tensors), non-contiguous inputs and outputs are handled
 instead of rejected or mis-written, and there is no 512-angle limit.
 
-Host arrays in z_order 0 (numpy or CPU tensors, with a host container or
-none) go through the library's host-buffer entry points
-(``vp_forward_z0_host`` / ``vp_backward_z0_host``), which overlap the
-copies to and from the GPU with the projection; the reference copies,
-projects and copies back one after another.  Page-locked CPU tensors
+Host arrays (numpy or CPU tensors, with a host container or none) go
+through the library's host-buffer entry points (``vp_forward_z0_host`` /
+``vp_backward_z0_host``, ``vp_forward_z2_host`` / ``vp_backward_z2_host``),
+which overlap the copies to and from the GPU with the projection; the
+reference copies, projects and copies back one after another.  Page-locked CPU tensors
 (``tensor.pin_memory()``) give the most overlap.
 """
 
@@ -161,8 +161,8 @@ def forward(x, angles, y, z_order=0, block_size=[8, 8, 8]):
     project = {0: forward_z0, 2: forward_z2}
     shape = default_shape[z_order]
     fn = project[z_order]
-    if z_order == 0 and kind != "cuda" and _host_out(y):
-        return _host_call("vp_forward_z0_host", x, y, angles, shape, kind)
+    if kind != "cuda" and _host_out(y):
+        return _host_call("vp_forward_z%d_host" % z_order, x, y, angles, shape, kind)
     x_gpu = _input_gpu(x)
     a_gpu = _angles_gpu(angles)
     y_gpu = gpu_array_with_default_shape(y, shape=shape)
@@ -181,8 +181,8 @@ def backward(y, angles, x, z_order=0, block_size=[8, 8, 8]):
     project = {0: backward_z0, 2: backward_z2}
     shape = default_shape[z_order]
     fn = project[z_order]
-    if z_order == 0 and kind != "cuda" and _host_out(x):
-        return _host_call("vp_backward_z0_host", y, x, angles, shape, kind)
+    if kind != "cuda" and _host_out(x):
+        return _host_call("vp_backward_z%d_host" % z_order, y, x, angles, shape, kind)
     y_gpu = _input_gpu(y)
     a_gpu = _angles_gpu(angles)
     x_gpu = gpu_array_with_default_shape(x, shape=shape)

@@ -68,7 +68,12 @@ cudaError_t get_ctx(int nev, HostCtx** out) {
   if (c.copy_in == nullptr) {
     if ((e = cudaStreamCreateWithFlags(&c.copy_in, cudaStreamNonBlocking)) != cudaSuccess)
       return e;
-    if ((e = cudaStreamCreateWithFlags(&c.copy_out, cudaStreamNonBlocking)) != cudaSuccess)
+    // the out stream's small add kernels must not wait behind the projection's
+    // blocks: highest priority
+    int least = 0, greatest = 0;
+    if ((e = cudaDeviceGetStreamPriorityRange(&least, &greatest)) != cudaSuccess) return e;
+    if ((e = cudaStreamCreateWithPriority(&c.copy_out, cudaStreamNonBlocking, greatest)) !=
+        cudaSuccess)
       return e;
     if ((e = cudaStreamCreateWithFlags(&c.compute2, cudaStreamNonBlocking)) != cudaSuccess)
       return e;

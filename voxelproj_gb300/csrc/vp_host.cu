@@ -267,12 +267,17 @@ cudaError_t forward_z0_host(const float* x_host, float* y_host, const float* ang
     for (int j = 0; j + 1 < ncpieces; ++j)
       VP_TRY(launch_forward_z0_stream(xd, yd, ad, gs, 0, 0, ccut[j], ccut[j + 1], 0, g.n_ang, 1,
                                       s, launches));
+    // the angle groups of the last block are independent (disjoint angles):
+    // alternate them over the two kernel streams so their last waves overlap
+    VP_TRY(cudaEventRecord(ev_out, s));
+    VP_TRY(cudaStreamWaitEvent(c->compute2, ev_out, 0));
     for (int j = 0; j < ngroups; ++j) {
       const int a0 = (int)((long long)g.n_ang * j / ngroups);
       const int a1 = (int)((long long)g.n_ang * (j + 1) / ngroups);
+      const cudaStream_t sj = (j & 1) ? c->compute2 : s;
       VP_TRY(launch_forward_z0_stream(xd, yd, ad, gs, 0, 0, ccut[ncpieces - 1],
-                                      ccut[ncpieces], a0, a1, 1, s, launches));
-      VP_TRY(cudaEventRecord(ev_group[j], s));
+                                      ccut[ncpieces], a0, a1, 1, sj, launches));
+      VP_TRY(cudaEventRecord(ev_group[j], sj));
       VP_TRY(cudaStreamWaitEvent(c->copy_out, ev_group[j], 0));
       const size_t off = (size_t)a0 * ang_elems, n = (size_t)(a1 - a0) * ang_elems;
       if (g.accumulate) {
@@ -284,6 +289,7 @@ cudaError_t forward_z0_host(const float* x_host, float* y_host, const float* ang
     }
     VP_TRY(cudaEventRecord(ev_out, c->copy_out));
     return cudaStreamWaitEvent(s, ev_out, 0);  // s ends after the last angles are home
+                                               // (and so after compute2's groups)
   }, s);
 }
 

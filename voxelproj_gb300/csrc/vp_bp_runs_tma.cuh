@@ -79,68 +79,6 @@ __device__ __forceinline__ void run_window_staged(float4x2 (&acc)[RUN], const fl
   }
 }
 
-// The class's angles in [w0, wend), ascending, into list; returns the count.
-template <int PASS>
-__device__ __forceinline__ int list_class_angles(const float* angles, int w0, int wend,
-                                                 int trig, int* list) {
-  const int lane = threadIdx.x & 31;
-  int nlist = 0;
-  for (int a1 = w0; a1 < wend; a1 += 32) {
-    const int a = a1 + lane;
-    const bool mine = a < wend && in_class<PASS>(angles[a], trig);
-    const unsigned mask = __ballot_sync(0xffffffffu, mine);
-    if (mine) list[nlist + __popc(mask & ((1u << lane) - 1u))] = a;
-    nlist += __popc(mask);
-  }
-  __syncwarp();
-  return nlist;
-}
-
-// The table entry of bp_runs_warp for angle a and the run at (xi0, yi0).
-template <int PASS>
-__device__ __forceinline__ RunEntry run_entry(const float* angles, int a, const Geom& g,
-                                              int xi0, int yi0) {
-  const int dx = PASS == 0 ? 1 : 0;
-  const int dy = PASS == 0 ? 0 : 1;
-  const AngleConst k = angle_const(angles[a], g.trig);
-  BinWeights bw[RUN];
-#pragma unroll
-  for (int m = 0; m < RUN; ++m) {
-    const float relx = (float)(xi0 + m * dx) - g.xcent;
-    const float rely = (float)(yi0 + m * dy) - g.ycent;
-    bw[m] = voxel_weights(relx, rely, k, g.pcent, g.trig);
-  }
-  const float step = PASS == 0 ? k.c : k.s;
-  const int dir = step >= 0.0f ? 1 : -1;
-  int pattern = 0;
-  bool ok = true;
-#pragma unroll
-  for (int m = 0; m + 1 < RUN; ++m) {
-    const int d = dir * (bw[m + 1].r - bw[m].r);
-    ok = ok && (d == 0 || d == 1);
-    pattern |= (d == 1 ? 1 : 0) << m;
-  }
-  const int base = bw[0].r - dir;
-  const int last = base + dir * (2 + __popc(pattern));
-  ok = ok && (unsigned)base < (unsigned)g.PX && (unsigned)last < (unsigned)g.PX;
-  float ws[12];
-#pragma unroll
-  for (int m = 0; m < RUN; ++m) {
-    ws[3 * m + 0] = dir > 0 ? bw[m].w0 : bw[m].w2;
-    ws[3 * m + 1] = bw[m].w1;
-    ws[3 * m + 2] = dir > 0 ? bw[m].w2 : bw[m].w0;
-  }
-  RunEntry e;
-  e.w[0] = make_float4(ws[0], ws[1], ws[2], ws[3]);
-  e.w[1] = make_float4(ws[4], ws[5], ws[6], ws[7]);
-  e.w[2] = make_float4(ws[8], ws[9], ws[10], ws[11]);
-  e.r = make_int4(bw[0].r, bw[1].r, bw[2].r, bw[3].r);
-  const long long off = (long long)a * g.PX * g.Hy + (long long)base * g.Hy;
-  e.meta = make_int4((int)(unsigned)(off & 0xffffffffll), (int)(off >> 32), dir * g.Hy,
-                     ok ? pattern : BPR_GENERIC);
-  return e;
-}
-
 // Window bins [first, last] (ascending) of a fast entry.
 __device__ __forceinline__ void window_bins(const RunEntry& e, int* first, int* last) {
   const int dir = e.meta.z >= 0 ? 1 : -1;

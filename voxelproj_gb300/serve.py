@@ -4,22 +4,27 @@ Requests (a sinogram, its angles, the volume shape, an iteration count and a
 method) arrive over time.  The server keeps every admitted request's volume,
 sinogram and iterates resident on the device.  A request is admitted when its
 device footprint fits the memory budget and a slot is free; otherwise it
-waits in arrival order.  Each scheduler tick advances every active request by
-one iteration:
-  * one batched launch computes A p for all of them, together with A 1 for
-    requests admitted this tick (SIRT's row sums);
+waits, in arrival order (policy "fifo") or shortest total work first
+(policy "sjf": iterations x voxels x angles, known on arrival).  Each
+scheduler tick advances every active request by one iteration:
+  * A p for all of them, together with A 1 for requests admitted this tick
+    (SIRT's row sums);
   * per-request elementwise steps run as fused multi-tensor ops;
-  * one batched launch computes A^T r for all of them, together with A^T 1
-    (SIRT's column sums) or A^T b (CGLS's first direction) for new requests.
+  * A^T r for all of them, together with A^T 1 (SIRT's column sums) or
+    A^T b (CGLS's first direction) for new requests.
+Requests small enough that one of them leaves the GPU partly idle share one
+batched launch per direction; requests that fill the GPU on their own run
+the single-problem kernels (launch "auto"; "batch" puts every request in the
+batch).
 Finished requests retire at the end of the tick, which frees their slot and
 memory for the queue.  The batched launches reproduce the single-problem
 kernels bit for bit, and each request's elementwise steps are its own, so a
 result does not depend on the other requests in the mix
 (tests/test_serve_gpu.py).
 
-The batches run on the persistent kernel of vp_batch_run (voxelproj_gb300.batch);
-their plans are cached per set of active requests and rebuilt when the set
-changes.
+The batches run on the persistent kernels of vp_batch_run
+(voxelproj_gb300.batch); their plans are cached per set of batched requests
+and rebuilt when the set changes.
 
     python -m voxelproj_gb300.serve [--requests 24] [--rate 200]
 
@@ -98,9 +103,20 @@ class ReconstructionServer:
     number of active requests.  `clock` returns seconds and defines request
     arrival and completion times."""
 
-    def __init__(self, budget_bytes: int, max_active: int = 64, device="cuda", clock=None):
+    # a request whose A call has at least this many voxel x angle updates
+    # fills the GPU on its own (several waves of blocks at 512^2 x 128 heights)
+    LARGE_VU = 1 << 31
+
+    def __init__(self, budget_bytes: int, max_active: int = 64, device="cuda", clock=None,
+                 policy: str = "fifo", launch: str = "auto"):
+        if policy not in ("fifo", "sjf"):
+            raise ValueError(policy)
+        if launch not in ("auto", "batch"):
+            raise ValueError(launch)
         self.budget = int(budget_bytes)
         self.max_active = max_active
+        self.policy = policy
+        self.launch = launch
         self.device = torch.device(device)
         self.clock = clock or time.perf_counter
         self.queue: list = []      # heap of (arrival, rid, request)
@@ -121,12 +137,31 @@ class ReconstructionServer:
                              f"more than the budget {self.budget}")
         heapq.heappush(self.queue, (req.arrival, req.rid, req))
 
+    @staticmethod
+    def work(req: Request) -> int:
+        """Voxel x angle updates of the whole solve (two per iteration)."""
+        return 2 * req.iters * int(np.prod(req.vol_shape)) * int(req.angles.numel())
+
+    def _next(self, now: float):
+        """Index in the queue of the request to admit next, or None."""
+        if not self.queue or self.queue[0][0] > now:
+            return None
+        if self.policy == "fifo":
+            return 0
+        arrived = [i for i, (t, _, _) in enumerate(self.queue) if t <= now]
+        return min(arrived, key=lambda i: (self.work(self.queue[i][2]), self.queue[i][1]))
+
     def _admit(self, now: float) -> None:
         while self.queue and len(self.active) < self.max_active:
-            arrival, _, req = self.queue[0]
-            if arrival > now or self.in_use + req.footprint() > self.budget:
-                return  # arrival order: the head waits for memory, later ones wait too
-            heapq.heappop(self.queue)
+            i = self._next(now)
+            if i is None:
+                return
+            req = self.queue[i][2]
+            if self.in_use + req.footprint() > self.budget:
+                return  # the chosen request waits for memory, later ones wait too
+            self.queue[i] = self.queue[-1]
+            self.queue.pop()
+            heapq.heapify(self.queue)
             req.admitted = now
             self.in_use += req.footprint()
             st = _State(req)
@@ -154,15 +189,19 @@ class ReconstructionServer:
             self._plans[key] = plan
         return plan
 
+    def _large(self, req: Request) -> bool:
+        return (self.launch == "auto" and
+                int(np.prod(req.vol_shape)) * int(req.angles.numel()) >= self.LARGE_VU)
+
     def _forward_problems(self):
         probs = []
         for st in self.active:
             r, b = st.req, st.bufs
             if r.method == "sirt":
                 src, dst = (b["ones_x"], b["R"]) if st.fresh else (b["x"], b["ax"])
-                probs.append(("forward", src, dst, r.angles))
+                probs.append((st, ("forward", src, dst, r.angles)))
             elif not st.fresh:
-                probs.append(("forward", b["p"], b["q"], r.angles))
+                probs.append((st, ("forward", b["p"], b["q"], r.angles)))
         return probs
 
     def _backward_problems(self):
@@ -171,10 +210,25 @@ class ReconstructionServer:
             r, b = st.req, st.bufs
             if r.method == "sirt":
                 src, dst = (b["ones_y"], b["C"]) if st.fresh else (b["r"], b["g"])
-                probs.append(("backward", src, dst, r.angles))
+                probs.append((st, ("backward", src, dst, r.angles)))
             else:
-                probs.append(("backward", b["r"], b["s"], r.angles))
+                probs.append((st, ("backward", b["r"], b["s"], r.angles)))
         return probs
+
+    def _project(self, tag: str, probs) -> None:
+        """Large requests through the single-problem kernels, the rest in one
+        batched launch (plan cached per set of batched requests)."""
+        from . import _CU
+
+        small = []
+        for st, (op, src, dst, ang) in probs:
+            if self._large(st.req):
+                (_CU.forward_z0 if op == "forward" else _CU.backward_z0)(src, dst, ang)
+            else:
+                small.append((st, (op, src, dst, ang)))
+        if small:
+            key = (tag,) + tuple((st.req.rid, st.fresh) for st, _ in small)
+            self._plan(key, [p for _, p in small]).run()
 
     # -- one tick ------------------------------------------------------------
     def step(self) -> None:
@@ -183,7 +237,6 @@ class ReconstructionServer:
         if not self.active:
             return
         self.ticks += 1
-        key = tuple((st.req.rid, st.fresh) for st in self.active)
         sirt_run = [st for st in self.active if st.req.method == "sirt" and not st.fresh]
         sirt_new = [st for st in self.active if st.req.method == "sirt" and st.fresh]
         cgls_run = [st for st in self.active if st.req.method == "cgls" and not st.fresh]
@@ -192,9 +245,7 @@ class ReconstructionServer:
         # outputs are accumulated into: clear them first
         _zero([st.bufs["ax"] for st in sirt_run] + [st.bufs["R"] for st in sirt_new]
               + [st.bufs["q"] for st in cgls_run])
-        fwd = self._forward_problems()
-        if fwd:
-            self._plan(("F",) + key, fwd).run()
+        self._project("F", self._forward_problems())
 
         # SIRT: r = R (b - A x); new: R = 1 / (A 1) where positive
         if sirt_run:
@@ -216,9 +267,7 @@ class ReconstructionServer:
 
         _zero([st.bufs["g"] for st in sirt_run] + [st.bufs["C"] for st in sirt_new]
               + [st.bufs["s"] for st in cgls_run + cgls_new])
-        bwd = self._backward_problems()
-        if bwd:
-            self._plan(("B",) + key, bwd).run()
+        self._project("B", self._backward_problems())
 
         # SIRT: x += C A^T r; new: C = 1 / (A^T 1) where positive
         if sirt_run:
@@ -321,12 +370,17 @@ def main() -> None:
     ap.add_argument("--max-active", type=int, default=64)
     ap.add_argument("--min-side", type=int, default=128)
     ap.add_argument("--max-side", type=int, default=512)
+    ap.add_argument("--policy", choices=("fifo", "sjf"), default="fifo",
+                    help="admission order: arrival, or shortest total work first")
+    ap.add_argument("--launch", choices=("auto", "batch"), default="auto",
+                    help="auto: requests that fill the GPU run single-problem kernels")
     args = ap.parse_args()
     reqs = make_requests(args.requests, args.rate, sides=(args.min_side, args.max_side))
     torch.cuda.synchronize()
 
     # served, continuous batching
-    srv = ReconstructionServer(int(args.budget_gb * 2**30), args.max_active)
+    srv = ReconstructionServer(int(args.budget_gb * 2**30), args.max_active,
+                               policy=args.policy, launch=args.launch)
     t0 = time.perf_counter()
     srv.clock = lambda: time.perf_counter() - t0
     for r in reqs:
@@ -352,6 +406,7 @@ def main() -> None:
                     "iterations U{20..100}",
         "served": served_stats, "plain_sequential": plain_stats,
         "solves_per_s_ratio": round(served_stats["solves_per_s"] / plain_stats["solves_per_s"], 3),
+        "policy": args.policy, "launch": args.launch,
         "ticks": srv.ticks, "voxel_angle_updates": vu,
         "served_gvu_s": round(vu / served_stats["makespan_s"] / 1e9, 1),
     }))

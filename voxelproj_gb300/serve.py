@@ -30,11 +30,10 @@ and rebuilt when the set changes.
 
 runs the served-SIRT workload: Poisson arrivals (default mean 200 per
 second), ellipsoid phantoms with side U{128..512} (multiples of 4), U{128..1024}
-angles and U{20..100} SIRT iterations, served with 2 active requests admitted
-shortest work first (the best measured: these requests fill the GPU, so more
-concurrency only delays every one of them).  It reports p50/p99 latency and
+angles and U{20..100} SIRT iterations.  It reports p50/p99 latency and
 solves per second for the server, and for the same requests solved one by one
-in arrival order with plain calls.  It prints one JSON line.
+with plain calls in arrival order and in shortest-work order.  It prints one
+JSON line.
 
 No counterpart in the reference, which provides only A and A^T.
 """
@@ -369,18 +368,42 @@ def main() -> None:
     ap.add_argument("--requests", type=int, default=24)
     ap.add_argument("--rate", type=float, default=200.0)
     ap.add_argument("--budget-gb", type=float, default=96.0)
-    ap.add_argument("--max-active", type=int, default=2)
+    ap.add_argument("--max-active", type=int, default=64)
     ap.add_argument("--min-side", type=int, default=128)
     ap.add_argument("--max-side", type=int, default=512)
-    ap.add_argument("--policy", choices=("fifo", "sjf"), default="sjf",
+    ap.add_argument("--policy", choices=("fifo", "sjf"), default="fifo",
                     help="admission order: arrival, or shortest total work first")
     ap.add_argument("--launch", choices=("auto", "batch"), default="auto",
                     help="auto: requests that fill the GPU run single-problem kernels")
+    ap.add_argument("--warmup-s", type=float, default=10.0,
+                    help="untimed projections before the timed phases (a fresh GPU "
+                         "runs slower for its first tens of seconds under load)")
     args = ap.parse_args()
     reqs = make_requests(args.requests, args.rate, sides=(args.min_side, args.max_side))
     torch.cuda.synchronize()
 
+    # warm-up: A and A^T on a mid-sized problem for warmup_s seconds
+    if args.warmup_s > 0:
+        from . import _CU
+
+        wx = torch.randn(384, 384, 384, device="cuda")
+        wy = torch.zeros(256, 384, 384, device="cuda")
+        wa = torch.linspace(0, np.pi, 257, device="cuda")[:-1].contiguous()
+        t_end = time.perf_counter() + args.warmup_s
+        while time.perf_counter() < t_end:
+            _CU.forward_z0(wx, wy, wa)
+            _CU.backward_z0(wy, wx, wa)
+            torch.cuda.synchronize()
+        del wx, wy, wa
+
+    # every phase starts with torch's allocator cache empty, so none reuses
+    # the blocks another phase allocated
+    def cold() -> None:
+        torch.cuda.synchronize()
+        torch.cuda.empty_cache()
+
     # served, continuous batching
+    cold()
     srv = ReconstructionServer(int(args.budget_gb * 2**30), args.max_active,
                                policy=args.policy, launch=args.launch)
     t0 = time.perf_counter()
@@ -390,16 +413,30 @@ def main() -> None:
     served = srv.run()
     served_stats = _latency_stats(served, 0.0)
 
-    # plain sequential calls, same arrivals
-    t0 = time.perf_counter()
-    for r in reqs:
-        now = time.perf_counter() - t0
-        if now < r.arrival:
-            time.sleep(r.arrival - now)
-        solve_plain(r)
-        torch.cuda.synchronize()
-        r.finished = time.perf_counter() - t0
-    plain_stats = _latency_stats(reqs, 0.0)
+    # plain sequential calls, same arrivals: in arrival order, and shortest
+    # work first among the arrived requests (the server's ordering, without
+    # the server)
+    def plain(order: str) -> dict:
+        pending = sorted(reqs, key=lambda r: r.arrival)
+        t0 = time.perf_counter()
+        while pending:
+            now = time.perf_counter() - t0
+            arrived = [r for r in pending if r.arrival <= now]
+            if not arrived:
+                time.sleep(max(0.0, pending[0].arrival - now))
+                continue
+            r = arrived[0] if order == "fifo" else min(
+                arrived, key=lambda q: (ReconstructionServer.work(q), q.rid))
+            pending.remove(r)
+            solve_plain(r)
+            torch.cuda.synchronize()
+            r.finished = time.perf_counter() - t0
+        return _latency_stats(reqs, 0.0)
+
+    cold()
+    plain_stats = plain("fifo")
+    cold()
+    plain_sjf_stats = plain("sjf")
     vu = sum(2 * r.vol_shape[0] * r.vol_shape[1] * r.vol_shape[2] * r.angles.numel() * r.iters
              for r in reqs)
     print(json.dumps({
@@ -407,6 +444,7 @@ def main() -> None:
                     f"U{{{args.min_side}..{args.max_side}}}, angles U{{128..1024}}, "
                     "iterations U{20..100}",
         "served": served_stats, "plain_sequential": plain_stats,
+        "plain_sequential_shortest_first": plain_sjf_stats,
         "solves_per_s_ratio": round(served_stats["solves_per_s"] / plain_stats["solves_per_s"], 3),
         "policy": args.policy, "launch": args.launch,
         "ticks": srv.ticks, "voxel_angle_updates": vu,

@@ -14,6 +14,7 @@ constexpr int BPR_WARPS = 4;
 constexpr int BPR_CHUNK = 32;
 constexpr int BPR_LIST = 1024;  // class angles listed per window of the angle axis
 constexpr int BPR_GENERIC = 8;  // pattern value of the generic path
+constexpr int BPR_SKIP = 9;     // pattern value of a window wholly off the detector
 
 struct RunEntry {
   float4 w[3];  // weights of voxels 0..3, 3 each, in window order
@@ -24,7 +25,8 @@ struct RunEntry {
 
 // Fast path for advance pattern PAT: loads the W = 3 + popcount(PAT) window
 // bins with no predicates (the table phase routed windows that leave the
-// detector to the generic path), then applies the four voxels' weights.
+// detector to the generic path, and windows wholly off it to no path at all),
+// then applies the four voxels' weights.
 // p points at the window's first bin at this lane's first height (lh.s0);
 // stride is the signed distance between consecutive window bins.
 template <int PAT, int R>
@@ -121,6 +123,12 @@ __device__ __forceinline__ RunEntry run_entry(const float* angles, int a, const 
   const int base = bw[0].r - dir;
   const int last = base + dir * (2 + __popc(pattern));
   ok = ok && (unsigned)base < (unsigned)g.PX && (unsigned)last < (unsigned)g.PX;
+  // every bin of every voxel off the detector: the run adds nothing at this
+  // angle (adding the zero products would leave the sums unchanged, bit for
+  // bit, since a sum that starts at +0 never becomes -0)
+  const int rmin = min(min(bw[0].r, bw[1].r), min(bw[2].r, bw[3].r));
+  const int rmax = max(max(bw[0].r, bw[1].r), max(bw[2].r, bw[3].r));
+  const bool off_detector = rmax + 1 < 0 || rmin - 1 >= g.PX;
   float ws[12];
 #pragma unroll
   for (int m = 0; m < RUN; ++m) {
@@ -135,7 +143,7 @@ __device__ __forceinline__ RunEntry run_entry(const float* angles, int a, const 
   e.r = make_int4(bw[0].r, bw[1].r, bw[2].r, bw[3].r);
   const long long off = (long long)a * g.PX * g.Hy + (long long)base * g.Hy;
   e.meta = make_int4((int)(unsigned)(off & 0xffffffffll), (int)(off >> 32), dir * g.Hy,
-                     ok ? pattern : BPR_GENERIC);
+                     off_detector ? BPR_SKIP : ok ? pattern : BPR_GENERIC);
   return e;
 }
 
@@ -190,6 +198,7 @@ __device__ __forceinline__ void bp_runs_warp(const float* __restrict__ y, float*
           case 5: run_window<5, R>(acc, wv, p, stride, lh); break;
           case 6: run_window<6, R>(acc, wv, p, stride, lh); break;
           case 7: run_window<7, R>(acc, wv, p, stride, lh); break;
+          case BPR_SKIP: break;
           default: {
             // generic path: three guarded loads per voxel, bins relative to
             // the window start (p), whose bin is r0 - dir

@@ -85,6 +85,28 @@ def test_overwrite_mode_and_device_angles(geom):
         tol.ref_vs_fp64(max(SY, SX))
 
 
+@pytest.mark.parametrize("n", [1, 2, 3, 5])
+def test_host_entries_few_angles(n):
+    """Angle counts below the forward's two angle halves and four output
+    groups, and below the adjoint's first-angles split."""
+    SY, SX, H, PX = 40, 36, 264, 44
+    ang = lin(n, 0.1, 3.0)
+    x = torch.tensor(seeded((SY, SX, H), 41)).pin_memory()
+    y = torch.tensor(seeded((n, PX, H), 42)).pin_memory()
+    y0 = torch.tensor(seeded((n, PX, H), 43)).pin_memory()
+    x0 = torch.tensor(seeded((SY, SX, H), 44)).pin_memory()
+    a = torch.tensor(ang)
+    yo = y0.clone()
+    _call("vp_forward_z0_host", x, yo, a)
+    xo = x0.clone()
+    _call("vp_backward_z0_host", y, xo, a)
+    n_ext = max(SY, SX, PX)
+    assert rel_err(yo.numpy() - y0.numpy(), oracle.forward(x.numpy(), ang, PX, 0)) <= \
+        tol.ref_vs_fp64(n_ext)
+    assert rel_err(xo.numpy() - x0.numpy(), oracle.backward(y.numpy(), ang, SY, SX, 0)) <= \
+        tol.ref_vs_fp64(n_ext)
+
+
 def test_height_extents_differ():
     """H = min(Hx, Hy): heights past the shorter array stay as they were
     (accumulate) or become zero (overwrite)."""

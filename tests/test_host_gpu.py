@@ -107,6 +107,36 @@ def test_host_entries_few_angles(n):
         tol.ref_vs_fp64(n_ext)
 
 
+@pytest.mark.parametrize("trig", [0, 1])
+def test_host_forward_angles_near_the_class_boundary(trig):
+    """The host forward sends angles whose minor axis is x beyond doubt home
+    before the column blocks run.  Angles at and around 45 and 135 degrees
+    (inside and outside the margin), and large angles, must still come back
+    complete."""
+    offs = [0.0, 1e-6, -1e-6, 1e-4, -1e-4, 9e-4, -9e-4, 1.2e-3, -1.2e-3, 3e-3, -3e-3, 1e-2]
+    base = [np.pi / 4, 3 * np.pi / 4, -np.pi / 4, 5 * np.pi / 4]
+    ang = np.array([b + o for b in base for o in offs] + [15.0, -15.0, 15.7, 14.9, 0.0, 0.3],
+                   dtype=np.float32)
+    SY, SX, H, PX = 48, 40, 136, 60
+    x = torch.tensor(seeded((SY, SX, H), 45)).pin_memory()
+    y0 = torch.tensor(seeded((len(ang), PX, H), 46)).pin_memory()
+    yo = y0.clone()
+    flags = _lib.VP_FLAG_TRIG_PRECISE if trig else 0
+    _call("vp_forward_z0_host", x, yo, torch.tensor(ang), flags)
+    if trig:  # the fast sin/cos of the reference trig drift from FP64 at 15 rad
+        ref = oracle.forward(x.numpy(), ang, PX, 0)
+        assert rel_err(yo.numpy() - y0.numpy(), ref) <= tol.ref_vs_fp64(max(SY, SX, PX))
+    # the device path: the same kernels and classes (an angle sent home
+    # before its column blocks ran would differ by whole bins)
+    xd, yd, ad = x.cuda(), y0.cuda(), torch.tensor(ang, device="cuda")
+    _lib.check(_lib.LIB.vp_forward_z0(xd.data_ptr(), *xd.shape, yd.data_ptr(), *yd.shape,
+                                      ad.data_ptr(), len(ang), flags,
+                                      torch.cuda.current_stream().cuda_stream),
+               "vp_forward_z0")
+    torch.cuda.synchronize()
+    assert rel_err(yo.numpy(), yd.cpu().numpy()) <= 4e-6
+
+
 def test_height_extents_differ():
     """H = min(Hx, Hy): heights past the shorter array stay as they were
     (accumulate) or become zero (overwrite)."""

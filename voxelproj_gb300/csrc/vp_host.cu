@@ -38,6 +38,7 @@
 // (voxelproj/wrappers.py:10-25 and :57-73).
 #include <cuda_runtime.h>
 
+#include <cmath>
 #include <cstdint>
 #include <mutex>
 #include <vector>
@@ -51,6 +52,11 @@ namespace {
 constexpr int kMaxDevices = 64;
 constexpr int kAdjointSlabs = 16;     // adjoint row slabs per call
 constexpr int kForwardAngleGroups = 4;  // groups of the forward's last slab
+// Forward angles sent home early: |phi| at most this many radians, and
+// |cos phi| - |sin phi| at least this margin, far above the error of the
+// kernels' single-precision sin/cos in that range.
+constexpr double kEarlyMaxRad = 16.0;
+constexpr double kEarlyMargin = 1e-3;
 
 // Side streams and events of one device, created on first use and kept.
 struct HostCtx {
@@ -231,16 +237,33 @@ cudaError_t forward_z0_host(const float* x_host, float* y_host, const float* ang
     // wave overlaps the other chain's next launch
     const int nhalves = g.n_ang >= 2 ? 2 : 1;
     const int ah[3] = {0, nhalves == 2 ? g.n_ang / 2 : g.n_ang, g.n_ang};
+    // Angles whose minor axis is x beyond doubt are final once every row
+    // piece and the remainder heights have run, so they go back while the
+    // column blocks run; the others go back in groups of the last column
+    // block.  The kernels classify with single-precision sin/cos, within far
+    // less than the margin of double precision here.
+    std::vector<char> early(g.n_ang, 0);
+    if (!is_device_pointer(angles)) {
+      for (int a = 0; a < g.n_ang; ++a) {
+        const double phi = angles[a];
+        if (std::fabs(phi) <= kEarlyMaxRad)
+          early[a] = std::fabs(std::cos(phi)) - std::fabs(std::sin(phi)) >= kEarlyMargin;
+      }
+    }
+    std::vector<int> late[2];
+    for (int h = 0; h < nhalves; ++h)
+      for (int a = ah[h]; a < ah[h + 1]; ++a)
+        if (!early[a]) late[h].push_back(a);
     // output groups of the last column block, per half
     const int per_half = kForwardAngleGroups / 2;
     int ng[2] = {0, 0};
     for (int h = 0; h < nhalves; ++h)
-      ng[h] = ah[h + 1] - ah[h] < per_half ? ah[h + 1] - ah[h] : per_half;
+      ng[h] = (int)late[h].size() < per_half ? (int)late[h].size() : per_half;
     HostCtx* c = nullptr;
-    VP_TRY(get_ctx(npieces + ng[0] + ng[1] + 5, &c));
+    VP_TRY(get_ctx(npieces + ng[0] + ng[1] + 7, &c));
     cudaEvent_t ev_alloc = c->ev[0], ev_cont = c->ev[1], ev_out = c->ev[2], ev_c2 = c->ev[3],
-                ev_rest = c->ev[4];
-    cudaEvent_t* ev_piece = c->ev.data() + 5;
+                ev_rest = c->ev[4], ev_rows1 = c->ev[5], ev_c2end = c->ev[6];
+    cudaEvent_t* ev_piece = c->ev.data() + 7;
     cudaEvent_t* ev_group = ev_piece + npieces;
 
     // the side streams start after the allocations (and prior work) on s
@@ -261,6 +284,17 @@ cudaError_t forward_z0_host(const float* x_host, float* y_host, const float* ang
     VP_TRY(cudaEventRecord(ev_cont, c->copy_in));
     VP_TRY(cudaStreamWaitEvent(c->copy_out, ev_cont, 0));
 
+    // angles [a0, a1) are final: add the container and send them home
+    auto send = [&](int a0, int a1) -> cudaError_t {
+      const size_t off = (size_t)a0 * ang_elems, n = (size_t)(a1 - a0) * ang_elems;
+      if (g.accumulate) {
+        VP_TRY(launch_add(yd + off, yc + off, n, c->copy_out));
+        *launches += 1;
+      }
+      return cudaMemcpyAsync(y_host + off, yd + off, n * sizeof(float), cudaMemcpyDefault,
+                             c->copy_out);
+    };
+
     Geom gs = g;
     gs.accumulate = 0;
     if (g.H < g.Hy) {  // heights past x's extent are not written: start from zero
@@ -279,40 +313,57 @@ cudaError_t forward_z0_host(const float* x_host, float* y_host, const float* ang
                                         ah[h + 1], k == 0 ? gs.accumulate : 1, st[h],
                                         launches));
       }
+    VP_TRY(cudaEventRecord(ev_rows1, c->compute2));
     // every row is in: the remainder heights (other heights than the chains
-    // write), then the other angles on blocks of columns
+    // write), then the early angles go home
     VP_TRY(launch_forward_z0_rest(xd, yd, ad, gs, s, launches));
     VP_TRY(cudaEventRecord(ev_rest, s));
+    VP_TRY(cudaStreamWaitEvent(c->copy_out, ev_rest, 0));
+    VP_TRY(cudaStreamWaitEvent(c->copy_out, ev_rows1, 0));
+    for (int a = 0; a < g.n_ang;) {
+      if (!early[a]) {
+        ++a;
+        continue;
+      }
+      int e = a;
+      while (e < g.n_ang && early[e]) ++e;
+      VP_TRY(send(a, e));
+      a = e;
+    }
+    // the other angles on blocks of columns
     for (int j = 0; j + 1 < ncpieces; ++j)
       for (int h = 0; h < nhalves; ++h)
         VP_TRY(launch_forward_z0_stream(xd, yd, ad, gs, 0, 0, ccut[j], ccut[j + 1], ah[h],
                                         ah[h + 1], 1, st[h], launches));
-    // the last block by angle groups, each group sent back once final (and
-    // once the remainder heights, on s, are written)
+    // the last block by groups of the late angles (equal counts), each group
+    // sent home once final (and once the remainder heights, on s, are
+    // written)
     VP_TRY(cudaStreamWaitEvent(c->compute2, ev_rest, 0));
     int gi = 0;
     for (int j = 0; j < per_half; ++j)
       for (int h = 0; h < nhalves; ++h) {
         if (j >= ng[h]) continue;
-        const int span = ah[h + 1] - ah[h];
-        const int a0 = ah[h] + (int)((long long)span * j / ng[h]);
-        const int a1 = ah[h] + (int)((long long)span * (j + 1) / ng[h]);
+        const int m = (int)late[h].size();
+        const int i0 = (int)((long long)m * j / ng[h]);
+        const int i1 = (int)((long long)m * (j + 1) / ng[h]);
         VP_TRY(launch_forward_z0_stream(xd, yd, ad, gs, 0, 0, ccut[ncpieces - 1],
-                                        ccut[ncpieces], a0, a1, 1, st[h], launches));
+                                        ccut[ncpieces], late[h][i0], late[h][i1 - 1] + 1, 1,
+                                        st[h], launches));
         VP_TRY(cudaEventRecord(ev_group[gi], st[h]));
         VP_TRY(cudaStreamWaitEvent(c->copy_out, ev_group[gi], 0));
         ++gi;
-        const size_t off = (size_t)a0 * ang_elems, n = (size_t)(a1 - a0) * ang_elems;
-        if (g.accumulate) {
-          VP_TRY(launch_add(yd + off, yc + off, n, c->copy_out));
-          *launches += 1;
+        for (int i = i0; i < i1;) {  // runs of consecutive late angles
+          int e = i + 1;
+          while (e < i1 && late[h][e] == late[h][e - 1] + 1) ++e;
+          VP_TRY(send(late[h][i], late[h][e - 1] + 1));
+          i = e;
         }
-        VP_TRY(cudaMemcpyAsync(y_host + off, yd + off, n * sizeof(float), cudaMemcpyDefault,
-                               c->copy_out));
       }
+    // s ends after the last angles are home and compute2's work is done
+    VP_TRY(cudaEventRecord(ev_c2end, c->compute2));
+    VP_TRY(cudaStreamWaitEvent(s, ev_c2end, 0));
     VP_TRY(cudaEventRecord(ev_out, c->copy_out));
-    return cudaStreamWaitEvent(s, ev_out, 0);  // s ends after the last angles are home
-                                               // (and so after compute2's groups)
+    return cudaStreamWaitEvent(s, ev_out, 0);
   }, s);
 }
 

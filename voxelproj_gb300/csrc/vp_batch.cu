@@ -175,11 +175,12 @@ __host__ __device__ inline int body_of(const BatchDesc& d) {
 }
 
 // Resident blocks per SM the registers must allow, so that each body keeps
-// about its single-problem kernel's occupancy despite the item bookkeeping:
-// 8-height forward 6 (79 registers), 4-height forward 7 (72), 8-height run
+// its single-problem kernel's occupancy despite the item bookkeeping:
+// 8-height forward 7 (72 registers, a few spilled; at 6 blocks the 64-cube
+// batch took 332 ms instead of 322), 4-height forward 7 (72), 8-height run
 // adjoint 5 (96); the 4-height adjoints as the compiler chooses (72).
 constexpr int batch_min_blocks(int body) {
-  return body == B_FWD8 ? 6 : body == B_FWD4 ? 7 : body == B_BWD8 ? 5 : 0;
+  return body == B_FWD8 ? 7 : body == B_FWD4 ? 7 : body == B_BWD8 ? 5 : 0;
 }
 
 template <int BODY>

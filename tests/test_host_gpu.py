@@ -233,6 +233,26 @@ def test_z2_host_entries(geom):
     assert not yw[H:].any()
 
 
+@pytest.mark.parametrize("H", [100, 600])
+def test_z2_host_overwrite_sinogram_larger_than_volume(H):
+    """Out = result through the chunked pipeline, where a chunk of the
+    sinogram (90 angles x 40 bins) is larger than a chunk of the volume
+    (20 x 24), and back; two and three height chunks."""
+    SY, SX, n, PX = 20, 24, 90, 40
+    ang = lin(n, -0.4, 3.5)
+    x = torch.tensor(seeded((H, SY, SX), 51)).pin_memory()
+    y = torch.tensor(seeded((H, n, PX), 52)).pin_memory()
+    a = torch.tensor(ang)
+    yw = torch.full((H, n, PX), 9.0).pin_memory()
+    _call("vp_forward_z2_host", x, yw, a, _lib.VP_FLAG_OVERWRITE)
+    xw = torch.full((H, SY, SX), -2.0)
+    _call("vp_backward_z2_host", y, xw, a, _lib.VP_FLAG_OVERWRITE)
+    n_ext = max(SY, SX, PX)
+    assert rel_err(yw.numpy(), oracle.forward(x.numpy(), ang, PX, 2)) <= tol.ref_vs_fp64(n_ext)
+    assert rel_err(xw.numpy(), oracle.backward(y.numpy(), ang, SY, SX, 2)) <= \
+        tol.ref_vs_fp64(n_ext)
+
+
 def test_wrappers_take_the_host_path_for_z2():
     SY, SX, H, n = 30, 30, 40, 25
     ang = lin(n)

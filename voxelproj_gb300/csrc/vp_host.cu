@@ -470,11 +470,16 @@ cudaError_t backward_z0_host(const float* y_host, float* x_host, const float* an
 }
 
 // z_order 2 with host arrays.  Heights are the slowest axis of both arrays,
-// so a chunk of heights is a contiguous, independent problem.  Chunks
-// alternate between two kernel streams; each chunk's copies in, projection
-// (the device z_order 2 path) and copy out run on its stream, so one chunk's
-// copies overlap the other chunk's kernels.  Chunks of 256 heights (the
-// 8-heights-per-lane kernels' chunk) from 512 heights up, else halves.
+// so a chunk of heights is a contiguous, independent problem.  Chunks of 256
+// heights (the 8-heights-per-lane kernels' chunk) from 512 heights up, else
+// halves.  With the transposed path (32 heights and more):
+//   copy stream:  chunk inputs in order, each container after the next
+//                 chunk's input (the projections need only their inputs)
+//   kernel streams (alternating by chunk, one projection at a time): the
+//                 input to height-fastest order and its z_order 0 projection
+//   out stream:   per chunk, once projected and its container is in: the
+//                 transpose-add into the container, and home
+// Small heights run the native z_order 2 kernels per chunk on one stream.
 cudaError_t z2_host(bool forward, const float* in_host, float* out_host, const float* angles,
                     const Geom& g, cudaMemPool_t pool, cudaStream_t s, int* launches) {
   std::lock_guard<std::mutex> lock(g_mutex);
@@ -493,6 +498,7 @@ cudaError_t z2_host(bool forward, const float* in_host, float* out_host, const f
   return guarded([&]() -> cudaError_t {
     float *in_d[2] = {}, *out_d[2] = {}, *ws[2] = {}, *as = nullptr;
     const float* ad = nullptr;
+    const bool pipelined = z2_uses_transpose(gc);
     const size_t ws_elems = z2_workspace_bytes(gc) / sizeof(float);
     const int slots = nchunks > 1 ? 2 : 1;
     for (int i = 0; i < slots; ++i) {
@@ -502,38 +508,95 @@ cudaError_t z2_host(bool forward, const float* in_host, float* out_host, const f
     }
     VP_TRY(alloc_angles(angles, g, buf, pool, &ad, &as));
     HostCtx* c = nullptr;
-    VP_TRY(get_ctx(2, &c));
-    cudaEvent_t ev_ready = c->ev[0], ev_c2 = c->ev[1];
+    VP_TRY(get_ctx(4 * nchunks + 3, &c));
+    cudaEvent_t ev_ready = c->ev[0], ev_c2 = c->ev[1], ev_out = c->ev[2];
+    cudaEvent_t* ev_in = c->ev.data() + 3;    // chunk k's input is in
+    cudaEvent_t* ev_kern = ev_in + nchunks;   // chunk k's projection is in ws
+    cudaEvent_t* ev_cont = ev_kern + nchunks; // chunk k's container is in
+    cudaEvent_t* ev_done = ev_cont + nchunks; // chunk k is home
     VP_TRY(copy_angles(as, angles, g, s));
     VP_TRY(cudaEventRecord(ev_ready, s));  // buffers allocated, angles in
     VP_TRY(cudaStreamWaitEvent(c->compute2, ev_ready, 0));
     const cudaStream_t st[2] = {s, c->compute2};
-    for (int k = 0; k < nchunks; ++k) {
-      const cudaStream_t t = st[k & 1];
-      float* in_k = in_d[k & 1];
-      float* out_k = out_d[k & 1];
-      const int h0 = k * Hc;
-      const int hc = h0 + Hc <= H ? Hc : H - h0;
+    auto chunk = [&](int k) {
       Geom gk = g;
-      gk.H = gk.Hx = gk.Hy = hc;
-      gk.accumulate = 1;  // into the container's chunk, or zeros
-      VP_TRY(cudaMemcpyAsync(in_k, in_host + (size_t)h0 * in_per_h,
-                             (size_t)hc * in_per_h * sizeof(float), cudaMemcpyDefault, t));
-      if (g.accumulate)
-        VP_TRY(cudaMemcpyAsync(out_k, out_host + (size_t)h0 * out_per_h,
-                               (size_t)hc * out_per_h * sizeof(float), cudaMemcpyDefault, t));
-      else
-        VP_TRY(cudaMemsetAsync(out_k, 0, (size_t)hc * out_per_h * sizeof(float), t));
-      if (z2_uses_transpose(gk)) {
-        VP_TRY(forward ? forward_z2_transposed(in_k, out_k, ad, gk, ws[k & 1], t)
-                       : backward_z2_transposed(in_k, out_k, ad, gk, ws[k & 1], t));
-      } else {
-        VP_TRY(forward ? launch_forward_z2(in_k, out_k, ad, gk, t)
-                       : launch_backward_z2(in_k, out_k, ad, gk, t));
+      const int h0 = k * Hc;
+      gk.H = gk.Hx = gk.Hy = h0 + Hc <= H ? Hc : H - h0;
+      gk.accumulate = 1;
+      return gk;
+    };
+    if (!pipelined) {
+      // small heights (one chunk): the native z_order 2 kernels add into the
+      // container (or zeros) on the device
+      for (int k = 0; k < nchunks; ++k) {
+        const cudaStream_t t = st[k & 1];
+        const Geom gk = chunk(k);
+        const size_t h0 = (size_t)k * Hc, hc = (size_t)gk.H;
+        VP_TRY(cudaMemcpyAsync(in_d[k & 1], in_host + h0 * in_per_h,
+                               hc * in_per_h * sizeof(float), cudaMemcpyDefault, t));
+        if (g.accumulate)
+          VP_TRY(cudaMemcpyAsync(out_d[k & 1], out_host + h0 * out_per_h,
+                                 hc * out_per_h * sizeof(float), cudaMemcpyDefault, t));
+        else
+          VP_TRY(cudaMemsetAsync(out_d[k & 1], 0, hc * out_per_h * sizeof(float), t));
+        VP_TRY(forward ? launch_forward_z2(in_d[k & 1], out_d[k & 1], ad, gk, t)
+                       : launch_backward_z2(in_d[k & 1], out_d[k & 1], ad, gk, t));
+        *launches += launches_z2(gk, forward);
+        VP_TRY(cudaMemcpyAsync(out_host + h0 * out_per_h, out_d[k & 1],
+                               hc * out_per_h * sizeof(float), cudaMemcpyDefault, t));
       }
-      *launches += launches_z2(gk, forward);
-      VP_TRY(cudaMemcpyAsync(out_host + (size_t)h0 * out_per_h, out_k,
-                             (size_t)hc * out_per_h * sizeof(float), cudaMemcpyDefault, t));
+    } else {
+      // Inputs come in chunk by chunk ahead of their containers; the
+      // projections run one after another, alternating kernel streams; each
+      // chunk's way back (container, transpose-add, copy home) runs on the
+      // out stream once its projection and container are there.
+      VP_TRY(cudaStreamWaitEvent(c->copy_in, ev_ready, 0));
+      VP_TRY(cudaStreamWaitEvent(c->copy_out, ev_ready, 0));
+      auto issue_cont = [&](int j) -> cudaError_t {
+        if (!g.accumulate) return cudaSuccess;
+        if (j >= 2) VP_TRY(cudaStreamWaitEvent(c->copy_in, ev_done[j - 2], 0));  // slot free
+        const size_t h0 = (size_t)j * Hc, hc = (size_t)chunk(j).H;
+        VP_TRY(cudaMemcpyAsync(out_d[j & 1], out_host + h0 * out_per_h,
+                               hc * out_per_h * sizeof(float), cudaMemcpyDefault, c->copy_in));
+        return cudaEventRecord(ev_cont[j], c->copy_in);
+      };
+      auto issue_out = [&](int j) -> cudaError_t {
+        const Geom gj = chunk(j);
+        const size_t h0 = (size_t)j * Hc, hc = (size_t)gj.H;
+        VP_TRY(cudaStreamWaitEvent(c->copy_out, ev_kern[j], 0));
+        float* dst = out_d[j & 1];  // the container's chunk, or stored into
+        if (g.accumulate) VP_TRY(cudaStreamWaitEvent(c->copy_out, ev_cont[j], 0));
+        VP_TRY(z2_transpose_out(forward, dst, gj, ws[j & 1], g.accumulate ? 1 : 0,
+                                c->copy_out));
+        VP_TRY(cudaMemcpyAsync(out_host + h0 * out_per_h, dst, hc * out_per_h * sizeof(float),
+                               cudaMemcpyDefault, c->copy_out));
+        return cudaEventRecord(ev_done[j], c->copy_out);
+      };
+      for (int k = 0; k < nchunks; ++k) {
+        const cudaStream_t t = st[k & 1];
+        const Geom gk = chunk(k);
+        const size_t h0 = (size_t)k * Hc, hc = (size_t)gk.H;
+        // the input slot is free once chunk k - 2 is home (its projection
+        // read it)
+        if (k >= 2) VP_TRY(cudaStreamWaitEvent(c->copy_in, ev_done[k - 2], 0));
+        VP_TRY(cudaMemcpyAsync(in_d[k & 1], in_host + h0 * in_per_h,
+                               hc * in_per_h * sizeof(float), cudaMemcpyDefault, c->copy_in));
+        VP_TRY(cudaEventRecord(ev_in[k], c->copy_in));
+        VP_TRY(cudaStreamWaitEvent(t, ev_in[k], 0));
+        if (k >= 1) VP_TRY(cudaStreamWaitEvent(t, ev_kern[k - 1], 0));  // one at a time
+        if (k >= 2) VP_TRY(cudaStreamWaitEvent(t, ev_done[k - 2], 0));  // workspace free
+        VP_TRY(z2_project(forward, in_d[k & 1], ad, gk, ws[k & 1], t));
+        VP_TRY(cudaEventRecord(ev_kern[k], t));
+        *launches += launches_z2(gk, forward);
+        if (k >= 1) {
+          VP_TRY(issue_cont(k - 1));
+          VP_TRY(issue_out(k - 1));
+        }
+      }
+      VP_TRY(issue_cont(nchunks - 1));
+      VP_TRY(issue_out(nchunks - 1));
+      VP_TRY(cudaEventRecord(ev_out, c->copy_out));
+      VP_TRY(cudaStreamWaitEvent(s, ev_out, 0));
     }
     if (!g.accumulate && Hout > H) {
       // heights of the output past the input's extent: zero (out = result)

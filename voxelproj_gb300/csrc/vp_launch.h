@@ -39,6 +39,14 @@ cudaError_t forward_z2_transposed(const float* x, float* y, const float* angles,
                                   float* ws, cudaStream_t stream);
 cudaError_t backward_z2_transposed(const float* y, float* x, const float* angles, const Geom& g,
                                    float* ws, cudaStream_t stream);
+// The two halves of the transposed form: z2_project puts the input in
+// height-fastest order and stores its z_order 0 projection, both in ws;
+// z2_transpose_out adds (add = 1) or stores (0) that projection into the
+// caller's heights-slowest output.
+cudaError_t z2_project(bool forward, const float* in, const float* angles, const Geom& g,
+                       float* ws, cudaStream_t stream);
+cudaError_t z2_transpose_out(bool forward, float* out, const Geom& g, const float* ws, int add,
+                             cudaStream_t stream);
 
 // Height split of the 8-heights-per-lane forms: heights [0, r8_heights(H))
 // run with 8 per lane (chunks of 256); a last chunk of at most 128 heights

@@ -98,40 +98,55 @@ int launches_z2(const Geom& g, bool forward) {
                       : launches_backward_z0(aligned, aligned, g0));
 }
 
-// x (Hx, SY, SX) -> xt (SY, SX, Hp); yt = A xt; y (Hy, n, PX) += yt^T.
-cudaError_t forward_z2_transposed(const float* x, float* y, const float* angles, const Geom& g,
-                                  float* ws, cudaStream_t stream) {
+// The first steps of the transposed form, into ws: the input to
+// height-fastest order, then its z_order 0 projection (stored).
+//   forward:  x (Hx, SY, SX) -> xt (SY, SX, Hp); yt = A xt
+//   adjoint:  y (Hy, n, PX) -> yt (n, PX, Hp); xt = A^T yt
+cudaError_t z2_project(bool forward, const float* in, const float* angles, const Geom& g,
+                       float* ws, cudaStream_t stream) {
   const long long Hp = round4(g.H);
   const long long nvox = (long long)g.SY * g.SX;
   const long long nbin = (long long)g.n_ang * g.PX;
   float* xt = ws;
   float* yt = ws + nvox * Hp;
-  cudaError_t e = transpose(x, xt, g.H, nvox, nvox, Hp, 0, stream);
-  if (e != cudaSuccess) return e;
   Geom g0 = g;
   g0.H = g0.Hx = g0.Hy = (int)Hp;
   g0.accumulate = 0;
-  e = launch_forward_z0(xt, yt, angles, g0, stream);
+  if (forward) {
+    const cudaError_t e = transpose(in, xt, g.H, nvox, nvox, Hp, 0, stream);
+    if (e != cudaSuccess) return e;
+    return launch_forward_z0(xt, yt, angles, g0, stream);
+  }
+  const cudaError_t e = transpose(in, yt, g.H, nbin, nbin, Hp, 0, stream);
   if (e != cudaSuccess) return e;
-  return transpose(yt, y, nbin, g.H, Hp, nbin, 1, stream);
+  return launch_backward_z0(yt, xt, angles, g0, stream);
+}
+
+// The last step: out (+)= the projection in ws, back in heights-slowest
+// order (add = 1 adds, 0 stores).
+cudaError_t z2_transpose_out(bool forward, float* out, const Geom& g, const float* ws, int add,
+                             cudaStream_t stream) {
+  const long long Hp = round4(g.H);
+  const long long nvox = (long long)g.SY * g.SX;
+  const long long nbin = (long long)g.n_ang * g.PX;
+  if (forward) return transpose(ws + nvox * Hp, out, nbin, g.H, Hp, nbin, add, stream);
+  return transpose(ws, out, nvox, g.H, Hp, nvox, add, stream);
+}
+
+// x (Hx, SY, SX) -> xt (SY, SX, Hp); yt = A xt; y (Hy, n, PX) += yt^T.
+cudaError_t forward_z2_transposed(const float* x, float* y, const float* angles, const Geom& g,
+                                  float* ws, cudaStream_t stream) {
+  const cudaError_t e = z2_project(true, x, angles, g, ws, stream);
+  if (e != cudaSuccess) return e;
+  return z2_transpose_out(true, y, g, ws, 1, stream);
 }
 
 // y (Hy, n, PX) -> yt (n, PX, Hp); xt = A^T yt; x (Hx, SY, SX) += xt^T.
 cudaError_t backward_z2_transposed(const float* y, float* x, const float* angles, const Geom& g,
                                    float* ws, cudaStream_t stream) {
-  const long long Hp = round4(g.H);
-  const long long nvox = (long long)g.SY * g.SX;
-  const long long nbin = (long long)g.n_ang * g.PX;
-  float* xt = ws;
-  float* yt = ws + nvox * Hp;
-  cudaError_t e = transpose(y, yt, g.H, nbin, nbin, Hp, 0, stream);
+  const cudaError_t e = z2_project(false, y, angles, g, ws, stream);
   if (e != cudaSuccess) return e;
-  Geom g0 = g;
-  g0.H = g0.Hx = g0.Hy = (int)Hp;
-  g0.accumulate = 0;
-  e = launch_backward_z0(yt, xt, angles, g0, stream);
-  if (e != cudaSuccess) return e;
-  return transpose(xt, x, nvox, g.H, Hp, nvox, 1, stream);
+  return z2_transpose_out(false, x, g, ws, 1, stream);
 }
 
 }  // namespace vp

@@ -12,8 +12,10 @@
 //                 store mode into a fresh device y); once all rows are in, a
 //                 4-height remainder of split heights (main stream), then
 //                 the other angles on blocks of columns, the last block in
-//                 angle groups
-//   out stream:   per angle group, once final: y rows of those angles +=
+//                 groups of those angles
+//   out stream:   once all rows are in, the angles whose minor axis is x
+//                 beyond doubt (final then); later per group of the last
+//                 column block, once final: y rows of those angles +=
 //                 container, and back to the host
 //
 // Adjoint, x_host (+)= A^T y_host:

@@ -23,9 +23,11 @@
 // Stages.  The forward's volume slabs all add into the same sinogram bins,
 // and the run adjoint's two angle classes into the same voxels.  Within a
 // (problem, height chunk) these are numbered stages; every warp task counts
-// itself done on its stage's counter after writing, and a task of stage s > 0
-// waits, just before its read-modify-write, until stage s-1 is complete, then
-// reads the output past L1.  Items are taken in increasing order, so every
+// itself done after writing, and a task of stage s > 0 waits, just before its
+// read-modify-write, until what it adds to is complete, then reads the output
+// past L1: for the forward, the same output tile (height chunk, angle, bin
+// group) at stage s-1, on the tile's counter; for the adjoint, all of stage
+// s-1, on the stage's counter.  Items are taken in increasing order, so every
 // task a waiter depends on was taken earlier by a block that is already
 // running: the wait always ends.  It is bounded anyway: after ~4 s of spinning
 // it records an error (vp_batch_error) and writes regardless.
@@ -69,7 +71,7 @@ struct BatchDesc {
   int kind;
   int R;                // heights per lane: 4, or 8 as two float4 128 apart
   int nstages;          // stages per chunk
-  int counter_base;     // first stage counter of this problem
+  int counter_base;     // first counter of this problem (forward: per tile; adjoints: per stage)
   // forward: slab plan (class slabs, rows and columns per slab), bin groups
   // per angle
   int cls, wy, wx, units;
@@ -113,6 +115,22 @@ struct StageWait {
   }
 };
 
+// A warp's wait state parked in shared memory while its body runs, so that
+// the gather does not hold it in registers.
+struct WaitSlot {
+  unsigned* counter;
+  int* error;
+  unsigned target;
+};
+
+struct SlotWait {
+  const WaitSlot* slot;
+  static constexpr bool coherent = true;
+  __device__ __forceinline__ void operator()() const {
+    if (slot->target > 0) StageWait{slot->counter, slot->target, slot->error}();
+  }
+};
+
 __device__ __forceinline__ void signal_done(unsigned* counter) {
   __syncwarp();
   if ((threadIdx.x & 31) == 0) {
@@ -121,24 +139,26 @@ __device__ __forceinline__ void signal_done(unsigned* counter) {
   }
 }
 
+// A forward item's outputs are the bins of one (height chunk, angle, bin
+// group) tile, written by one item per stage; its counter counts the warps
+// done on the tile, so a stage waits for the tile's previous stage alone.
 template <int R>
 __device__ __forceinline__ void run_fwd_item(const BatchDesc& d, int stage, int in_stage,
-                                             int hc, BatchSmem& sm, int w, int lane,
-                                             unsigned* counters, int* error) {
+                                             int hc, BatchSmem& sm, WaitSlot* slot, int w,
+                                             int lane, unsigned* counters, int* error) {
   constexpr int UN = R == 8 ? 2 : FP0_UNROLL;  // as the single-problem kernels
   const int a = in_stage / d.units;
   const int bg = in_stage - a * d.units;
   const Slab slab = slab_of(stage, d.cls, d.wy, d.wx, d.g.SY, d.g.SX);
-  unsigned* ctr = counters + d.counter_base + hc * d.nstages + stage;
+  if (lane == 0)
+    *slot = WaitSlot{counters + d.counter_base + ((size_t)hc * d.g.n_ang + a) * d.units + bg,
+                     error, (unsigned)(stage * BATCH_WARPS)};
+  __syncwarp();
   const int p0 = (bg * BATCH_WARPS + w) * 4;
   const int h = hc * 32 * R + lane * 4;
-  if (stage == 0) {
-    fp_z0_warp<R, 4, UN>(d.in, d.out, d.angles, d.g, p0, a, h, slab, 1, sm.cand[w]);
-  } else {
-    const StageWait wt{ctr - 1, (unsigned)(d.g.n_ang * d.units * BATCH_WARPS), error};
-    fp_z0_warp<R, 4, UN>(d.in, d.out, d.angles, d.g, p0, a, h, slab, 1, sm.cand[w], wt);
-  }
-  signal_done(ctr);
+  fp_z0_warp<R, 4, UN>(d.in, d.out, d.angles, d.g, p0, a, h, slab, 1, sm.cand[w],
+                       SlotWait{slot});
+  signal_done(slot->counter);
 }
 
 template <int R>
@@ -189,6 +209,7 @@ __global__ void __launch_bounds__(BATCH_THREADS, batch_min_blocks(BODY))
                  unsigned long long* __restrict__ next, unsigned* __restrict__ counters,
                  int* __restrict__ error) {
   __shared__ BatchSmem sm;
+  __shared__ WaitSlot slots[BATCH_WARPS];
   __shared__ long long s_item;
   const int w = threadIdx.x >> 5;
   const int lane = threadIdx.x & 31;
@@ -212,7 +233,8 @@ __global__ void __launch_bounds__(BATCH_THREADS, batch_min_blocks(BODY))
       constexpr int R = BODY == B_FWD8 ? 8 : 4;
       const int per_stage = d.g.n_ang * d.units;
       const int stage = in_chunk / per_stage;
-      run_fwd_item<R>(d, stage, in_chunk - stage * per_stage, hc, sm, w, lane, counters, error);
+      run_fwd_item<R>(d, stage, in_chunk - stage * per_stage, hc, sm, &slots[w], w, lane,
+                      counters, error);
     } else if (BODY == B_BWD8 || d.kind == K_BWD_RUNS) {
       constexpr int R = BODY == B_BWD8 ? 8 : 4;
       const bool first = in_chunk < d.groups0;
@@ -306,8 +328,12 @@ int part_desc(const vp_batch_problem& p, const vp::Geom& g, const float* in, flo
   }
   const long long hch = (g.H + 32 * d->R - 1) / (32 * d->R);
   if (hch * d->per_chunk >= (1ll << 31)) return VP_ERR_BATCH;  // items indexed as int
-  d->begin = hch * d->per_chunk;              // item count, turned into offsets later
-  d->counter_base = (int)(hch * d->nstages);  // counter count, turned into offsets later
+  d->begin = hch * d->per_chunk;  // item count, turned into offsets later
+  // counter count, turned into offsets later: one per forward tile, one per
+  // stage of the adjoints
+  const long long nctr = d->kind == vp::K_FWD ? hch * g.n_ang * d->units : hch * d->nstages;
+  if (nctr >= (1ll << 31)) return VP_ERR_BATCH;
+  d->counter_base = (int)nctr;
   return VP_OK;
 }
 

@@ -40,3 +40,31 @@ def test_trig_mode_switch():
     vp.set_trig_mode("reference")
     with pytest.raises(ValueError):
         vp.set_trig_mode("fast")
+
+
+def test_angle_cache_reuses_device_copies_by_content():
+    """Host angles are copied to the device once per distinct content; an
+    array changed in place, another dtype with other values, or another
+    device is a new entry; the cache is bounded."""
+    import torch
+
+    from voxelproj_gb300 import wrappers as w
+
+    w._ANGLE_CACHE.clear()
+    a = np.linspace(0, np.pi, 7).astype(np.float32)
+    t1 = w.cached_angles(a, "cpu")
+    assert t1.dtype == torch.float32 and t1.shape == (7,)
+    assert w.cached_angles(a.copy(), "cpu") is t1          # same bytes
+    assert w.cached_angles(list(a), "cpu") is t1            # a list of the same values
+    ta = torch.tensor(a)                                    # a tensor already on the device:
+    assert torch.equal(w.cached_angles(ta, "cpu"), t1)      # used as it is, not cached
+    a[3] += 1e-3                                            # changed in place
+    t2 = w.cached_angles(a, "cpu")
+    assert t2 is not t1 and float(t2[3]) == float(np.float32(a[3]))
+    np.testing.assert_array_equal(t1.numpy()[[0, 1, 2, 4, 5, 6]], t2.numpy()[[0, 1, 2, 4, 5, 6]])
+    b = a.astype(np.float64)                                # same float32 values
+    assert w.cached_angles(b, "cpu") is t2
+    for k in range(w._ANGLE_CACHE_SIZE + 5):
+        w.cached_angles(np.full(3, k, np.float32), "cpu")
+    assert len(w._ANGLE_CACHE) == w._ANGLE_CACHE_SIZE
+    w._ANGLE_CACHE.clear()

@@ -19,7 +19,10 @@ Mirrors voxelproj/wrappers.py:10-122 of the reference:
 
 Beyond the reference: ``angles`` may also be a list or tuple (the reference
 accepted only arrays/tensors), non-contiguous inputs and outputs are handled
-instead of rejected or mis-written, and there is no 512-angle limit.
+instead of rejected or mis-written, and there is no 512-angle limit.  Host
+angle arrays are copied to the device once per distinct content and reused
+(``cached_angles``); the reference copies them on every call
+(wrappers.py:50).
 
 Host arrays (numpy or CPU tensors, with a host container or none) go
 through the library's host-buffer entry points (``vp_forward_z0_host`` /
@@ -30,6 +33,8 @@ reference copies, projects and copies back one after another.  Page-locked CPU t
 """
 
 from __future__ import annotations
+
+from collections import OrderedDict
 
 import numpy as np
 import torch
@@ -52,11 +57,38 @@ def gpu_array_with_default_shape(x=None, shape=None):
     raise TypeError("x must be None, a shape tuple, or an array/tensor")
 
 
-def _angles_gpu(angles) -> torch.Tensor:
-    if isinstance(angles, (list, tuple)):
-        angles = np.asarray(angles, dtype=np.float32)
-    a = gpu_array_with_default_shape(angles)
-    return a.reshape(-1).contiguous()
+# Device copies of host angle arrays, keyed on their exact float32 bytes and
+# the device: a caller that passes the same angles every call (the usual
+# iterative reconstruction) pays the host-to-device copy once.  An array
+# changed in place has other bytes, so it gets its own entry.
+_ANGLE_CACHE: "OrderedDict[tuple, torch.Tensor]" = OrderedDict()
+_ANGLE_CACHE_SIZE = 32
+
+
+def cached_angles(angles, device) -> torch.Tensor:
+    """``angles`` on ``device`` as a contiguous float32 vector.  A tensor
+    already there is used as it is; host angles (numpy, list, tuple, CPU
+    tensor) come from the cache."""
+    device = torch.device(device)
+    if isinstance(angles, torch.Tensor) and angles.device == device:
+        return angles.to(torch.float32).reshape(-1).contiguous()
+    if isinstance(angles, torch.Tensor):
+        angles = angles.detach().cpu().numpy()
+    arr = np.ascontiguousarray(np.asarray(angles, dtype=np.float32).reshape(-1))
+    key = (str(device), arr.tobytes())
+    t = _ANGLE_CACHE.get(key)
+    if t is not None:
+        _ANGLE_CACHE.move_to_end(key)
+        return t
+    t = torch.from_numpy(arr.copy()).to(device)
+    _ANGLE_CACHE[key] = t
+    while len(_ANGLE_CACHE) > _ANGLE_CACHE_SIZE:
+        _ANGLE_CACHE.popitem(last=False)
+    return t
+
+
+def _angles_gpu(angles, device) -> torch.Tensor:
+    return cached_angles(angles, device)
 
 
 def _input_gpu(v) -> torch.Tensor:
@@ -164,7 +196,7 @@ def forward(x, angles, y, z_order=0, block_size=[8, 8, 8]):
     if kind != "cuda" and _host_out(y):
         return _host_call("vp_forward_z%d_host" % z_order, x, y, angles, shape, kind)
     x_gpu = _input_gpu(x)
-    a_gpu = _angles_gpu(angles)
+    a_gpu = _angles_gpu(angles, x_gpu.device)
     y_gpu = gpu_array_with_default_shape(y, shape=shape)
     work = y_gpu if y_gpu.is_contiguous() else y_gpu.contiguous()
     fn(x_gpu, work, a_gpu, block_size=block_size)
@@ -184,7 +216,7 @@ def backward(y, angles, x, z_order=0, block_size=[8, 8, 8]):
     if kind != "cuda" and _host_out(x):
         return _host_call("vp_backward_z%d_host" % z_order, y, x, angles, shape, kind)
     y_gpu = _input_gpu(y)
-    a_gpu = _angles_gpu(angles)
+    a_gpu = _angles_gpu(angles, y_gpu.device)
     x_gpu = gpu_array_with_default_shape(x, shape=shape)
     work = x_gpu if x_gpu.is_contiguous() else x_gpu.contiguous()
     fn(y_gpu, work, a_gpu, block_size=block_size)

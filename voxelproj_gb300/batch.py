@@ -129,11 +129,19 @@ def main() -> None:
     ap.add_argument("--count", type=int, default=64)
     ap.add_argument("--reps", type=int, default=5)
     ap.add_argument("--no-tune", action="store_true")
+    ap.add_argument("--cubes", default=None,
+                    help="explicit cubes as side:angles,... instead of the seeded workload")
+    ap.add_argument("--only", choices=("both", "forward", "backward"), default="both",
+                    help="batch A of every cube, A^T of every sinogram, or both")
     args = ap.parse_args()
     from . import _CU, tune
 
     dev = torch.device("cuda")
-    shapes = uneven_cubes(args.count)
+    if args.cubes:
+        shapes = [tuple(int(v) for v in c.split(":")) for c in args.cubes.split(",")]
+    else:
+        shapes = uneven_cubes(args.count)
+    fwd, bwd = args.only in ("both", "forward"), args.only in ("both", "backward")
     g = torch.Generator(device=dev).manual_seed(7)
     problems, plain = [], []
     vu = 0
@@ -145,9 +153,12 @@ def main() -> None:
         x_out = torch.zeros(side, side, side, device=dev)
         vf = None if args.no_tune else tune.batch_variant("forward", side, n)
         vb = None if args.no_tune else tune.batch_variant("backward", side, n)
-        problems += [("forward", x, y_out, ang, vf), ("backward", y, x_out, ang, vb)]
+        if fwd:
+            problems.append(("forward", x, y_out, ang, vf))
+        if bwd:
+            problems.append(("backward", y, x_out, ang, vb))
         plain.append((x, y_out, y, x_out, ang))
-        vu += 2 * side**3 * n
+        vu += (int(fwd) + int(bwd)) * side**3 * n
     batch = Batch(problems)
     before = _lib.LIB.vp_launch_count()
     graph = batch.graph()
@@ -168,16 +179,21 @@ def main() -> None:
 
     def sequential():
         for x, y_out, y, x_out, ang in plain:
-            _CU.forward_z0(x, y_out, ang)
-            _CU.backward_z0(y, x_out, ang)
+            if fwd:
+                _CU.forward_z0(x, y_out, ang)
+            if bwd:
+                _CU.backward_z0(y, x_out, ang)
 
     t_seq = timed(sequential)
     before = _lib.LIB.vp_launch_count()
     sequential()
     seq_launches = _lib.LIB.vp_launch_count() - before
     print(json.dumps({
-        "workload": f"{args.count} cubes, sides {{64..384 step 32}}, U{{90..720}} angles each; "
-                    "A of every cube and A^T of every sinogram",
+        "workload": (f"cubes {args.cubes}" if args.cubes else
+                     f"{args.count} cubes, sides {{64..384 step 32}}, U{{90..720}} angles each")
+                    + {"both": "; A of every cube and A^T of every sinogram",
+                       "forward": "; A of every cube", "backward": "; A^T of every sinogram"}[
+                           args.only],
         "voxel_angle_updates": vu, "work_items": batch.work_items,
         "graph_ms": round(t_graph, 3), "graph_gvu_s": round(vu / t_graph / 1e6, 1),
         "sequential_ms": round(t_seq, 3), "sequential_gvu_s": round(vu / t_seq / 1e6, 1),

@@ -216,7 +216,9 @@ __global__ void __launch_bounds__(BATCH_THREADS, batch_min_blocks(BODY))
   for (;;) {
     if (threadIdx.x == 0) s_item = (long long)atomicAdd(next, 1ull);
     __syncthreads();
-    const long long item = s_item;
+    // the same for every lane: broadcast within the warp so that it is
+    // warp-uniform to the compiler as well
+    const long long item = __shfl_sync(0xffffffffu, s_item, 0);
     if (item >= total) return;  // block-uniform
     int lo = 0, hi = ndesc - 1;
     while (lo < hi) {

@@ -165,6 +165,11 @@ def test_batch_rejects_unsupported_problems():
         Batch([("forward", x, torch.zeros(10, 8, 6, device="cuda"), a)])
     with pytest.raises(KeyError):
         Batch([("sideways", x, x, a)])
+    # forward variant 13 (two warps per bin run) has no batched body: a
+    # batch could not reproduce it bit for bit, so it is refused
+    x4 = torch.zeros(8, 8, 8, device="cuda")
+    with pytest.raises(RuntimeError):
+        Batch([("forward", x4, torch.zeros(10, 8, 8, device="cuda"), a, 13)])
     empty = Batch([])
     empty.run()
     empty.close()

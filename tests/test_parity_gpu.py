@@ -186,7 +186,7 @@ def test_backward_variants_store_mode_via_z2(variant, H):
     assert rel_err(outs[0] - x0, oracle.backward(y, ang, SY, SX, 2)) <= tol.ref_vs_fp64(PX)
 
 
-@pytest.mark.parametrize("variant", [1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12])
+@pytest.mark.parametrize("variant", [1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12, 13])
 @pytest.mark.parametrize("geom", [(23, 37, 132, 61, 50, "wide"), (9, 6, 8, 40, 11, "axes"),
                                   (70, 64, 256, 96, 90, "rand"), (30, 21, 260, 33, 40, "rand"),
                                   (26, 31, 1024, 23, 36, "wide")],
@@ -214,7 +214,7 @@ def test_forward_variants(variant, geom):
     assert err <= tol.ref_vs_fp64(max(SY, SX, PX))
 
 
-@pytest.mark.parametrize("variant", [1, 5, 7, 8, 9, 12])
+@pytest.mark.parametrize("variant", [1, 5, 7, 8, 9, 12, 13])
 @pytest.mark.parametrize("H", [36, 260, 512])
 def test_forward_variants_store_mode_via_z2(variant, H):
     """The forward's first slab launch writes the z_order 2 scratch in store

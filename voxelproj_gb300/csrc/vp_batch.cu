@@ -296,7 +296,8 @@ int part_desc(const vp_batch_problem& p, const vp::Geom& g, const float* in, flo
   if (p.op == VP_OP_FORWARD) {
     // the single-problem forward's plan for this variant (0: its default)
     const vp::Fp0Plan pl = vp::forward_z0_plan(g, true, p.variant);
-    if (pl.KW != 4 || pl.agroup || (pl.R == 8 ? pl.un != 2 : pl.un != vp::detail::FP0_UNROLL))
+    if (pl.KW != 4 || pl.agroup || pl.split ||
+        (pl.R == 8 ? pl.un != 2 : pl.un != vp::detail::FP0_UNROLL))
       return VP_ERR_BATCH;  // bodies the batch does not carry
     d->kind = vp::K_FWD;
     d->R = pl.R;

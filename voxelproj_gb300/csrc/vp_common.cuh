@@ -302,4 +302,15 @@ struct NoWait {
   static constexpr bool coherent = false;
 };
 
+// Pre-store hook of a block whose warps write the same outputs in two
+// rounds: the second round waits at the block barrier that the first round
+// reaches after writing (the writes are visible to the block after it).
+struct HalfBarrier {
+  bool second;
+  __device__ __forceinline__ void operator()() const {
+    if (second) __syncthreads();
+  }
+  static constexpr bool coherent = false;
+};
+
 }  // namespace vp

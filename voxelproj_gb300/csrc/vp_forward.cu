@@ -31,18 +31,36 @@ using namespace detail;
 // vp_fp_z0.cuh).  Blocks of FP0_WARPS warps take neighbouring bin runs of one
 // angle, or with AGROUP one bin run of neighbouring angles; blockIdx.z is the
 // height chunk of 32 * R heights.
-template <int R, int KW, bool AGROUP, int UN>
-__global__ void __launch_bounds__(32 * FP0_WARPS)
+// With SPLIT a block takes 2 bin runs instead of 4, each by 2 warps that
+// gather half of the slab's major lines each: twice the blocks, each half as
+// long, so the last wave of a launch leaves less of the GPU idle.  The first
+// half writes (in the caller's mode); after a block barrier the second adds.
+template <int R, int KW, bool AGROUP, int UN, bool SPLIT = false>
+__global__ void __launch_bounds__(32 * FP0_WARPS, SPLIT ? (R == 8 ? 7 : 8) : 0)
     fp_z0_kernel(const float* __restrict__ x, float* __restrict__ y,
                  const float* __restrict__ angles, Geom g, int a_base, Slab slab,
                  int accumulate) {
   __shared__ float4 cand[FP0_WARPS][32 * Fp0Cap<KW>::value];
   const int lane = threadIdx.x;
   const int w = threadIdx.y;
-  const int p0 = (AGROUP ? blockIdx.x : blockIdx.x * FP0_WARPS + w) * KW;
-  const int a = a_base + (AGROUP ? blockIdx.y * FP0_WARPS + w : blockIdx.y);
   const int h = blockIdx.z * 32 * R + lane * (R == 8 ? 4 : R);
-  fp_z0_warp<R, KW, UN>(x, y, angles, g, p0, a, h, slab, accumulate, cand[w]);
+  if constexpr (SPLIT) {
+    static_assert(!AGROUP && FP0_WARPS == 4, "two bin runs x two halves");
+    const int p0 = (blockIdx.x * 2 + (w & 1)) * KW;
+    const int a = a_base + blockIdx.y;
+    const int ym = slab.y_lo + (slab.y_hi - slab.y_lo) / 2;
+    const int xm = slab.x_lo + (slab.x_hi - slab.x_lo) / 2;
+    const bool second = w >= 2;
+    const Slab hs = second ? Slab{ym, slab.y_hi, xm, slab.x_hi, slab.yy_lo, slab.yy_hi}
+                           : Slab{slab.y_lo, ym, slab.x_lo, xm, slab.yy_lo, slab.yy_hi};
+    fp_z0_warp<R, KW, UN>(x, y, angles, g, p0, a, h, hs, second ? 1 : accumulate, cand[w],
+                          HalfBarrier{second});
+    if (!second) __syncthreads();  // the second half adds after this one wrote
+  } else {
+    const int p0 = (AGROUP ? blockIdx.x : blockIdx.x * FP0_WARPS + w) * KW;
+    const int a = a_base + (AGROUP ? blockIdx.y * FP0_WARPS + w : blockIdx.y);
+    fp_z0_warp<R, KW, UN>(x, y, angles, g, p0, a, h, slab, accumulate, cand[w]);
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -124,6 +142,7 @@ struct Fp0Config {
   int un;         // candidates loaded together
   int slab_mb;    // volume bytes of one height chunk per slab launch
   bool cls;       // class slabs (rows for one angle class, columns for the other)
+  bool split;     // two warps per bin run, each on half of the major lines
 };
 
 // Variants: 1 = 4 bins per warp, 4 heights per lane, warps of a block on
@@ -134,11 +153,12 @@ struct Fp0Config {
 // as 5 with class slabs of 32 / 64 / 128 MB (10 is the default: 11 runs 1%
 // faster at 512^3 with 192 angles but misses L2 on the volume, 5.3 against
 // 4.6 GB of DRAM traffic per call); 12 = as 1
-// with class slabs of 32 MB.  Heights not in float4 run the scalar form of
+// with class slabs of 32 MB; 13 = as 10 with two warps per bin run, each on
+// half of the slab's major lines (SPLIT).  Heights not in float4 run the scalar form of
 // the same bin layout; 8-height variants on problems of at most 128 heights
 // run the 4-height form.
 Fp0Config fp0_config(const Geom& g, bool vec4, int variant) {
-  Fp0Config c{vec4 ? 4 : 1, 4, false, FP0_UNROLL, 32, false};
+  Fp0Config c{vec4 ? 4 : 1, 4, false, FP0_UNROLL, 32, false, false};
   if (variant == 0) variant = 10;  // the default
   switch (variant) {
     case 2: c.KW = 8; break;
@@ -152,6 +172,7 @@ Fp0Config fp0_config(const Geom& g, bool vec4, int variant) {
     case 10: c.R = 8; c.un = 2; c.cls = true; c.slab_mb = 64; break;
     case 11: c.R = 8; c.un = 2; c.cls = true; c.slab_mb = 128; break;
     case 12: c.cls = true; break;
+    case 13: c.R = 8; c.un = 2; c.cls = true; c.slab_mb = 64; c.split = true; break;
     default: break;
   }
   if (c.R == 8 && (!vec4 || g.H <= 128)) {
@@ -227,7 +248,7 @@ struct SlabLaunch {
   int a_lo, a_hi;
 };
 
-template <int R, int KW, bool AGROUP, int UN>
+template <int R, int KW, bool AGROUP, int UN, bool SPLIT = false>
 cudaError_t launch_slab(const SlabLaunch& L, cudaStream_t stream, int* launches) {
   dim3 block(32, FP0_WARPS);
   const long long per_launch = AGROUP ? (long long)kMaxGridYZ * FP0_WARPS : kMaxGridYZ;
@@ -235,10 +256,12 @@ cudaError_t launch_slab(const SlabLaunch& L, cudaStream_t stream, int* launches)
   g.n_ang = L.a_hi;
   for (long long a_base = L.a_lo; a_base < L.a_hi; a_base += per_launch) {
     const long long na = L.a_hi - a_base < per_launch ? L.a_hi - a_base : per_launch;
-    const unsigned gx = AGROUP ? ceil_div(g.PX, KW) : ceil_div(g.PX, KW * FP0_WARPS);
+    const unsigned gx = AGROUP  ? ceil_div(g.PX, KW)
+                        : SPLIT ? ceil_div(g.PX, KW * 2)
+                                : ceil_div(g.PX, KW * FP0_WARPS);
     const unsigned gy = AGROUP ? ceil_div(na, FP0_WARPS) : (unsigned)na;
     dim3 grid(gx, gy, ceil_div(g.H, 32 * R));
-    fp_z0_kernel<R, KW, AGROUP, UN><<<grid, block, 0, stream>>>(L.x, L.y, L.angles, g,
+    fp_z0_kernel<R, KW, AGROUP, UN, SPLIT><<<grid, block, 0, stream>>>(L.x, L.y, L.angles, g,
                                                                 (int)a_base, L.slab,
                                                                 L.accumulate);
     if (launches) ++*launches;
@@ -261,9 +284,14 @@ cudaError_t launch_slab_r(const Fp0Config& c, const SlabLaunch& L, cudaStream_t 
 cudaError_t launch_slab_config(const Fp0Config& c, const SlabLaunch& L, cudaStream_t s, int* n) {
   if (c.R == 8) {
     if (c.KW == 8) return launch_slab<8, 8, false, 2>(L, s, n);
-    if (c.un == 2) return launch_slab<8, 4, false, 2>(L, s, n);
+    if (c.un == 2) {
+      if (c.split) return launch_slab<8, 4, false, 2, true>(L, s, n);
+      return launch_slab<8, 4, false, 2>(L, s, n);
+    }
     return launch_slab<8, 4, false, 4>(L, s, n);
   }
+  if (c.R == 4 && c.split && c.KW == 4 && !c.agroup)
+    return launch_slab<4, 4, false, FP0_UNROLL, true>(L, s, n);
   if (c.R == 4) return launch_slab_r<4>(c, L, s, n);
   return launch_slab_r<1>(c, L, s, n);
 }
@@ -327,6 +355,7 @@ Fp0Plan forward_z0_plan(const Geom& g, bool vec4, int variant) {
   p.un = c.un;
   p.agroup = c.agroup;
   p.cls = c.cls;
+  p.split = c.split;
   p.nslabs = fp0_slabs(g, c);
   fp0_slab_widths(g, c, p.nslabs, &p.wy, &p.wx);
   return p;

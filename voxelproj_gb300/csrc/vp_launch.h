@@ -63,7 +63,7 @@ inline int r8_heights(int H) {
 // follows the same plan, so its results equal the single-problem kernel's.
 struct Fp0Plan {
   int R, KW, un;
-  bool agroup, cls;
+  bool agroup, cls, split;
   int nslabs, wy, wx;
 };
 Fp0Plan forward_z0_plan(const Geom& g, bool vec4, int variant);

@@ -157,11 +157,12 @@ __global__ void __launch_bounds__(32 * BPB_WARPS)
 // saw no angle of its class leaves x untouched (in store mode the first launch
 // always writes).
 // ---------------------------------------------------------------------------
-template <int PASS, int R>
+template <int PASS, int R, bool ADD = false>
 __global__ void __launch_bounds__(32 * BPR_WARPS, R == 8 ? 5 : 0)
     bp_z0_runs_kernel(const float* __restrict__ y, float* __restrict__ x,
                       const float* __restrict__ angles, Geom g, int nrun_major, int run_base,
-                      int run_end, int row_end, int accumulate) {
+                      int run_end, int row_end, int accumulate,
+                      const float* __restrict__ addend = nullptr) {
   __shared__ RunEntry tab[BPR_WARPS][BPR_CHUNK];
   __shared__ int alist[BPR_WARPS][BPR_LIST];
   const int lane = threadIdx.x;
@@ -171,8 +172,8 @@ __global__ void __launch_bounds__(32 * BPR_WARPS, R == 8 ? 5 : 0)
   int xi0, yi0;
   run_origin<PASS>(run, nrun_major, &xi0, &yi0);
   if (yi0 >= row_end) return;
-  bp_runs_warp<PASS, R>(y, x, angles, g, xi0, yi0, blockIdx.y * 32 * R + lane * 4, accumulate,
-                        tab[w], alist[w]);
+  bp_runs_warp<PASS, R, NoWait, ADD>(y, x, angles, g, xi0, yi0, blockIdx.y * 32 * R + lane * 4,
+                                     accumulate, tab[w], alist[w], NoWait(), addend);
 }
 
 // Bounded-wait timeouts of this library's kernels (0 in correct operation).
@@ -395,9 +396,12 @@ cudaError_t launch_bp_z0_runs_tma(const float* y, float* x, const float* angles,
 
 // Both class launches for the voxel rows [row_lo, row_hi); row_lo is a
 // multiple of RUN (class-1 runs span RUN rows).
+// With addend, the class-1 launch also adds addend (same layout as x) into the
+// rows it writes, after its own sums: x = (x + A^T y) + addend.
 template <int R>
 cudaError_t launch_bp_z0_runs(const float* y, float* x, const float* angles, const Geom& g,
-                              int row_lo, int row_hi, cudaStream_t stream) {
+                              int row_lo, int row_hi, cudaStream_t stream,
+                              const float* addend = nullptr) {
   dim3 block(32, BPR_WARPS);
   const unsigned hchunks = ceil_div(g.H, 32 * R);
   const int nmaj0 = (int)ceil_div(g.SX, RUN);
@@ -413,8 +417,13 @@ cudaError_t launch_bp_z0_runs(const float* y, float* x, const float* angles, con
   const long long b1 = (long long)(row_lo / RUN) * g.SX;
   const long long e1 = (long long)ceil_div(row_hi, RUN) * g.SX;
   if (e1 > b1) {
-    bp_z0_runs_kernel<1, R><<<dim3(ceil_div(e1 - b1, BPR_WARPS), hchunks), block, 0, stream>>>(
-        y, x, angles, g, g.SX, (int)b1, (int)e1, row_hi, 1);
+    const dim3 grid(ceil_div(e1 - b1, BPR_WARPS), hchunks);
+    if (addend)
+      bp_z0_runs_kernel<1, R, true><<<grid, block, 0, stream>>>(
+          y, x, angles, g, g.SX, (int)b1, (int)e1, row_hi, 1, addend);
+    else
+      bp_z0_runs_kernel<1, R><<<grid, block, 0, stream>>>(y, x, angles, g, g.SX, (int)b1,
+                                                          (int)e1, row_hi, 1);
     return cudaGetLastError();
   }
   return cudaSuccess;
@@ -426,19 +435,21 @@ int bp0_split(const Geom& g) { return g.H > 128 ? r8_heights(g.H) : 0; }
 
 cudaError_t launch_bp_z0_runs_split(const float* y, float* x, const float* angles,
                                     const Geom& g, int row_lo, int row_hi,
-                                    cudaStream_t stream, bool tma = false) {
+                                    cudaStream_t stream, bool tma = false,
+                                    const float* addend = nullptr) {
   const int H8 = bp0_split(g);
   if (H8 > 0) {
     Geom g8 = g;
     g8.H = H8;
     const cudaError_t e =
         tma ? launch_bp_z0_runs_tma(y, x, angles, g8, row_lo, row_hi, stream)
-            : launch_bp_z0_runs<8>(y, x, angles, g8, row_lo, row_hi, stream);
+            : launch_bp_z0_runs<8>(y, x, angles, g8, row_lo, row_hi, stream, addend);
     if (e != cudaSuccess || H8 == g.H) return e;
   }
   Geom g4 = g;
   g4.H = g.H - H8;
-  return launch_bp_z0_runs<4>(y + H8, x + H8, angles, g4, row_lo, row_hi, stream);
+  return launch_bp_z0_runs<4>(y + H8, x + H8, angles, g4, row_lo, row_hi, stream,
+                              addend ? addend + H8 : nullptr);
 }
 
 bool bp0_vec4(const float* y, const float* x, const Geom& g) {
@@ -505,6 +516,20 @@ cudaError_t launch_backward_z0_rows(const float* y, float* x, const float* angle
   const int v = kernel_variant(OP_BACKWARD_Z0);
   if (v == 6) return launch_bp_z0_runs<4>(y, x, angles, g, row_lo, row_hi, stream);
   return launch_bp_z0_runs_split(y, x, angles, g, row_lo, row_hi, stream, v == 9);
+}
+
+bool backward_z0_rows_can_add(const float* y, const float* x, const Geom& g) {
+  const int v = kernel_variant(OP_BACKWARD_Z0);
+  return bp0_vec4(y, x, g) && (v == 0 || v == 6 || v == 7);
+}
+
+cudaError_t launch_backward_z0_rows_add(const float* y, float* x, const float* angles,
+                                        const Geom& g, int row_lo, int row_hi,
+                                        const float* addend, cudaStream_t stream) {
+  if (!backward_z0_rows_can_add(y, x, g) || row_lo % RUN != 0) return cudaErrorInvalidValue;
+  if (kernel_variant(OP_BACKWARD_Z0) == 6)
+    return launch_bp_z0_runs<4>(y, x, angles, g, row_lo, row_hi, stream, addend);
+  return launch_bp_z0_runs_split(y, x, angles, g, row_lo, row_hi, stream, false, addend);
 }
 
 cudaError_t launch_backward_z2(const float* y, float* x, const float* angles, const Geom& g,

@@ -153,12 +153,13 @@ __device__ __forceinline__ RunEntry run_entry(const float* angles, int a, const 
 // tables.  All 32 lanes must call it together.  wait() runs (by the whole
 // warp) just before the outputs are written; with Wait::coherent the read of
 // the output bypasses L1.
-template <int PASS, int R = 4, class Wait = NoWait>
+template <int PASS, int R = 4, class Wait = NoWait, bool ADD = false>
 __device__ __forceinline__ void bp_runs_warp(const float* __restrict__ y, float* __restrict__ x,
                                              const float* __restrict__ angles, const Geom& g,
                                              int xi0, int yi0, int h, int accumulate,
                                              RunEntry* tab, int* alist,
-                                             const Wait& wait = Wait()) {
+                                             const Wait& wait = Wait(),
+                                             const float* __restrict__ addend = nullptr) {
   using V = typename Vec<R>::T;
   static_assert(R == 4 || R == 8, "heights per lane: 4 or 8");
   const int lane = threadIdx.x & 31;
@@ -228,7 +229,21 @@ __device__ __forceinline__ void bp_runs_warp(const float* __restrict__ y, float*
   }
 
   wait();
-  if (lh.v[0] && (seen > 0 || !accumulate)) {  // a lane past H has no second half either
+  if constexpr (ADD) {
+    // adding into x, then adding addend (same layout as x): (x + sums) + addend,
+    // as a write of the sums followed by a separate add of addend
+    if (lh.v[0]) {
+#pragma unroll
+      for (int m = 0; m < RUN; ++m) {
+        const int xi = xi0 + m * dx;
+        const int yi = yi0 + m * dy;
+        if (xi < g.SX && yi < g.SY) {
+          const size_t o = ((size_t)yi * g.SX + xi) * g.Hx;
+          add_lane<R>(x + o, addend + o, lh, acc[m], seen > 0);
+        }
+      }
+    }
+  } else if (lh.v[0] && (seen > 0 || !accumulate)) {  // a lane past H has no second half either
 #pragma unroll
     for (int m = 0; m < RUN; ++m) {
       const int xi = xi0 + m * dx;

@@ -296,6 +296,31 @@ __device__ __forceinline__ void store_lane(float* p, const LaneH<R>& lh,
   }
 }
 
+// One lane's heights of the output row at p: p = (p + v) + a when with_v,
+// else p = p + a (a: the addend row, same layout).
+template <int R>
+__device__ __forceinline__ void add_lane(float* p, const float* a, const LaneH<R>& lh,
+                                         const typename Vec<R>::T& v, bool with_v) {
+  if constexpr (R == 8) {
+    const float4* parts = reinterpret_cast<const float4*>(&v);
+#pragma unroll
+    for (int k = 0; k < LaneH<R>::NQ; ++k) {
+      if (lh.v[k]) {
+        float4* q = reinterpret_cast<float4*>(p + lh.h + k * kSecondHalf);
+        const float4 c = __ldg(reinterpret_cast<const float4*>(a + lh.h + k * kSecondHalf));
+        const float4 t = with_v ? f4_add(*q, parts[k]) : *q;
+        *q = f4_add(t, c);
+      }
+    }
+  } else if (lh.v[0]) {
+    using V = typename Vec<R>::T;
+    V* q = reinterpret_cast<V*>(p + lh.h);
+    const V c = *reinterpret_cast<const V*>(a + lh.h);
+    const V t = with_v ? f4_add(*q, v) : *q;
+    *q = f4_add(t, c);
+  }
+}
+
 // Pre-store hook that does nothing (single-problem kernels).
 struct NoWait {
   __device__ __forceinline__ void operator()() const {}

@@ -26,8 +26,9 @@
 //                 then the remaining angles in row slabs, alternating with a
 //                 second kernel stream so that one slab's last wave overlaps
 //                 the next slab
-//   out stream:   per row slab, once computed: x rows += container rows,
-//                 and back to the host
+//   out stream:   per row slab, once computed: x rows += container rows
+//                 (done by the slab's last kernel with the run kernels), and
+//                 back to the host
 //
 // Device buffers come from the library's stream-ordered pool, so repeated
 // calls reuse memory without going back to the driver.  Copies use
@@ -446,18 +447,26 @@ cudaError_t backward_z0_host(const float* y_host, float* x_host, const float* an
     VP_TRY(cudaStreamWaitEvent(s, ev_in, 0));
     VP_TRY(cudaEventRecord(ev_first, s));  // y is in and the first angles are launched
     VP_TRY(cudaStreamWaitEvent(c->compute2, ev_first, 0));
+    // the run kernels add the container's rows themselves, in the slab's last
+    // launch (the same sums, in the same order, as a separate add)
+    const bool fused_add = g.accumulate && backward_z0_rows_can_add(yd + y0, xd, g1);
     for (int k = 0; k < nslabs; ++k) {
       const int lo = k * rows;
       const int hi = lo + rows < g.SY ? lo + rows : g.SY;
       const cudaStream_t sk = (k & 1) ? c->compute2 : s;  // slabs write disjoint rows
-      VP_TRY(launch_backward_z0_rows(yd + y0, xd, ad + a_split, g1, lo, hi, sk));
+      if (fused_add) {
+        VP_TRY(cudaStreamWaitEvent(sk, ev_cont[k], 0));
+        VP_TRY(launch_backward_z0_rows_add(yd + y0, xd, ad + a_split, g1, lo, hi, xc, sk));
+      } else {
+        VP_TRY(launch_backward_z0_rows(yd + y0, xd, ad + a_split, g1, lo, hi, sk));
+      }
       *launches += launches_backward_z0(yd, xd, g1);
       VP_TRY(cudaEventRecord(ev_rows[k], sk));
-      // rows [lo, hi) are final: add the container's rows and send them back
+      // rows [lo, hi) are final: (add the container's rows and) send them back
       VP_TRY(cudaStreamWaitEvent(c->copy_out, ev_rows[k], 0));
       VP_TRY(cudaStreamWaitEvent(c->copy_out, ev_cont[k], 0));
       const size_t off = (size_t)lo * row_elems, n = (size_t)(hi - lo) * row_elems;
-      if (g.accumulate) {
+      if (g.accumulate && !fused_add) {
         VP_TRY(launch_add(xd + off, xc + off, n, c->copy_out));
         *launches += 1;
       }

@@ -93,6 +93,14 @@ unsigned long long wait_timeouts();
 cudaError_t launch_backward_z0_rows(const float* y, float* x, const float* angles,
                                     const Geom& g, int row_lo, int row_hi,
                                     cudaStream_t stream);
+// As launch_backward_z0_rows, and then adds addend (same layout as x) into
+// those rows: x = (x + A^T y) + addend in adding mode, A^T y + addend in
+// store mode, in the same order as a separate add after the projection.
+// Only for the run variants (backward_z0_rows_can_add).
+bool backward_z0_rows_can_add(const float* y, const float* x, const Geom& g);
+cudaError_t launch_backward_z0_rows_add(const float* y, float* x, const float* angles,
+                                        const Geom& g, int row_lo, int row_hi,
+                                        const float* addend, cudaStream_t stream);
 
 // Host-buffer projections (vp_host.cu): g.accumulate selects out += result
 // (1) or out = result (0); *launches is incremented by the kernels launched.

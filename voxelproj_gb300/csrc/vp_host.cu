@@ -19,7 +19,7 @@
 //                 container, and back to the host
 //
 // Adjoint, x_host (+)= A^T y_host:
-//   copy stream:  angles, the first eighth of the angles' sinogram rows,
+//   copy stream:  angles, the first sixth of the angles' sinogram rows,
 //                 the rest, then the x container slab by slab
 //   main stream:  the adjoint of the first angles over the whole volume as
 //                 soon as they are in (store mode into a fresh device x),
@@ -53,7 +53,7 @@ namespace vp {
 namespace {
 
 constexpr int kMaxDevices = 64;
-constexpr int kAdjointSlabs = 16;     // adjoint row slabs per call
+constexpr int kAdjointSlabs = 12;     // adjoint row slabs per call
 constexpr int kForwardAngleGroups = 4;  // groups of the forward's last slab
 // Forward angles sent home early: |phi| at most this many radians, and
 // |cos phi| - |sin phi| at least this margin, far above the error of the
@@ -393,11 +393,11 @@ cudaError_t backward_z0_host(const float* y_host, float* x_host, const float* an
       rows = (rows + step - 1) / step * step;
     }
     const int nslabs = (g.SY + rows - 1) / rows;
-    // the first eighth of the angles runs over the whole volume first, while
-    // the rest of the sinogram arrives (at 512^3 with 192 angles, 16 slabs
-    // and an eighth measured 6.5-6.7 ms per call against 6.96 ms with 8 slabs
-    // and a quarter)
-    const int a_split = g.n_ang >= 8 ? g.n_ang / 8 : 0;
+    // the first sixth of the angles runs over the whole volume first, while
+    // the rest of the sinogram arrives (at 512^3 with 192 angles, 12 slabs
+    // and a sixth measured 6.22 ms per call; 16 and an eighth 6.37 ms; 8 and
+    // a quarter 6.72 ms)
+    const int a_split = g.n_ang >= 8 ? g.n_ang / 6 : 0;
     HostCtx* c = nullptr;
     VP_TRY(get_ctx(2 * nslabs + 6, &c));
     cudaEvent_t ev_alloc = c->ev[0], ev_in0 = c->ev[1], ev_in = c->ev[2], ev_out = c->ev[3],

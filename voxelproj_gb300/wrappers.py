@@ -34,6 +34,7 @@ reference copies, projects and copies back one after another.  Page-locked CPU t
 
 from __future__ import annotations
 
+import threading
 from collections import OrderedDict
 
 import numpy as np
@@ -63,6 +64,7 @@ def gpu_array_with_default_shape(x=None, shape=None):
 # changed in place has other bytes, so it gets its own entry.
 _ANGLE_CACHE: "OrderedDict[tuple, torch.Tensor]" = OrderedDict()
 _ANGLE_CACHE_SIZE = 32
+_ANGLE_CACHE_LOCK = threading.Lock()
 
 
 def cached_angles(angles, device) -> torch.Tensor:
@@ -76,14 +78,16 @@ def cached_angles(angles, device) -> torch.Tensor:
         angles = angles.detach().cpu().numpy()
     arr = np.ascontiguousarray(np.asarray(angles, dtype=np.float32).reshape(-1))
     key = (str(device), arr.tobytes())
-    t = _ANGLE_CACHE.get(key)
-    if t is not None:
-        _ANGLE_CACHE.move_to_end(key)
-        return t
+    with _ANGLE_CACHE_LOCK:
+        t = _ANGLE_CACHE.get(key)
+        if t is not None:
+            _ANGLE_CACHE.move_to_end(key)
+            return t
     t = torch.from_numpy(arr.copy()).to(device)
-    _ANGLE_CACHE[key] = t
-    while len(_ANGLE_CACHE) > _ANGLE_CACHE_SIZE:
-        _ANGLE_CACHE.popitem(last=False)
+    with _ANGLE_CACHE_LOCK:
+        _ANGLE_CACHE[key] = t
+        while len(_ANGLE_CACHE) > _ANGLE_CACHE_SIZE:
+            _ANGLE_CACHE.popitem(last=False)
     return t
 
 

@@ -54,6 +54,7 @@ namespace {
 
 constexpr int kMaxDevices = 64;
 constexpr int kAdjointSlabs = 12;     // adjoint row slabs per call
+constexpr int kZ2AdjointSlabs = 8;    // row slabs of the z_order 2 adjoint's last chunk
 constexpr int kForwardAngleGroups = 4;  // groups of the forward's last slab
 // Forward angles sent home early: |phi| at most this many radians, and
 // |cos phi| - |sin phi| at least this margin, far above the error of the
@@ -518,17 +519,6 @@ cudaError_t z2_host(bool forward, const float* in_host, float* out_host, const f
       if (ws_elems > 0) VP_TRY(buf.get(pool, ws_elems * sizeof(float), &ws[i]));
     }
     VP_TRY(alloc_angles(angles, g, buf, pool, &ad, &as));
-    HostCtx* c = nullptr;
-    VP_TRY(get_ctx(4 * nchunks + 3, &c));
-    cudaEvent_t ev_ready = c->ev[0], ev_c2 = c->ev[1], ev_out = c->ev[2];
-    cudaEvent_t* ev_in = c->ev.data() + 3;    // chunk k's input is in
-    cudaEvent_t* ev_kern = ev_in + nchunks;   // chunk k's projection is in ws
-    cudaEvent_t* ev_cont = ev_kern + nchunks; // chunk k's container is in
-    cudaEvent_t* ev_done = ev_cont + nchunks; // chunk k is home
-    VP_TRY(copy_angles(as, angles, g, s));
-    VP_TRY(cudaEventRecord(ev_ready, s));  // buffers allocated, angles in
-    VP_TRY(cudaStreamWaitEvent(c->compute2, ev_ready, 0));
-    const cudaStream_t st[2] = {s, c->compute2};
     auto chunk = [&](int k) {
       Geom gk = g;
       const int h0 = k * Hc;
@@ -536,6 +526,60 @@ cudaError_t z2_host(bool forward, const float* in_host, float* out_host, const f
       gk.accumulate = 1;
       return gk;
     };
+    // the z_order 0 view of chunk 0's workspace, for the row pieces and slabs
+    Geom gw = chunk(0);
+    const size_t Hp0 = ((size_t)gw.H + 3) / 4 * 4;
+    gw.H = gw.Hx = gw.Hy = (int)Hp0;
+    gw.accumulate = 0;
+    std::vector<int> cut{0}, ccut{0}, scut{0};
+    if (pipelined && forward) {
+      float* xt0 = ws[0];
+      float* yt0 = ws[0] + vox * Hp0;
+      const int rows = forward_z0_stream_rows(xt0, yt0, gw);
+      const int cols = forward_z0_stream_cols(xt0, yt0, gw);
+      int r = rows / 4 >= 8 ? rows / 4 : rows;  // a quarter piece first
+      r = r < g.SY ? r : g.SY;
+      cut.push_back(r);
+      while (r < g.SY) {
+        r = r + rows < g.SY ? r + rows : g.SY;
+        cut.push_back(r);
+      }
+      for (int q = 0; q < g.SX;) {
+        q = q + cols < g.SX ? q + cols : g.SX;
+        ccut.push_back(q);
+      }
+    } else if (pipelined) {
+      const int last = (nchunks - 1) & 1;
+      Geom gl = chunk(nchunks - 1);
+      gl.H = gl.Hx = gl.Hy = (int)(((size_t)gl.H + 3) / 4 * 4);
+      const float* xtl = ws[last];
+      const int step = backward_z0_row_step(xtl + vox * gl.H, xtl, gl);
+      if (step > 0) {
+        int rows = (g.SY + kZ2AdjointSlabs - 1) / kZ2AdjointSlabs;
+        rows = (rows + step - 1) / step * step;
+        for (int q = 0; q < g.SY;) {
+          q = q + rows < g.SY ? q + rows : g.SY;
+          scut.push_back(q);
+        }
+      } else {
+        scut.push_back(g.SY);
+      }
+    }
+    const int npieces = (int)cut.size() - 1;
+    const int nslabs = (int)scut.size() - 1;
+    HostCtx* c = nullptr;
+    VP_TRY(get_ctx(4 * nchunks + 3 + npieces + nslabs, &c));
+    cudaEvent_t ev_ready = c->ev[0], ev_c2 = c->ev[1], ev_out = c->ev[2];
+    cudaEvent_t* ev_in = c->ev.data() + 3;    // chunk k's input is in
+    cudaEvent_t* ev_kern = ev_in + nchunks;   // chunk k's projection is in ws
+    cudaEvent_t* ev_cont = ev_kern + nchunks; // chunk k's container is in
+    cudaEvent_t* ev_done = ev_cont + nchunks; // chunk k is home
+    cudaEvent_t* ev_piece = ev_done + nchunks; // forward: row piece p of chunk 0 is in
+    cudaEvent_t* ev_slab = ev_piece + npieces; // adjoint: row slab r of the last chunk
+    VP_TRY(copy_angles(as, angles, g, s));
+    VP_TRY(cudaEventRecord(ev_ready, s));  // buffers allocated, angles in
+    VP_TRY(cudaStreamWaitEvent(c->compute2, ev_ready, 0));
+    const cudaStream_t st[2] = {s, c->compute2};
     if (!pipelined) {
       // small heights (one chunk): the native z_order 2 kernels add into the
       // container (or zeros) on the device
@@ -561,6 +605,10 @@ cudaError_t z2_host(bool forward, const float* in_host, float* out_host, const f
       // projections run one after another, alternating kernel streams; each
       // chunk's way back (container, transpose-add, copy home) runs on the
       // out stream once its projection and container are there.
+      // The forward's first chunk comes in by volume rows (strided copies)
+      // and is projected piece by piece as in the z_order 0 pipeline, so the
+      // kernels start early; the adjoint's last chunk is projected and sent
+      // home by row slabs, so that most of it is home when the kernels end.
       VP_TRY(cudaStreamWaitEvent(c->copy_in, ev_ready, 0));
       VP_TRY(cudaStreamWaitEvent(c->copy_out, ev_ready, 0));
       auto issue_cont = [&](int j) -> cudaError_t {
@@ -571,12 +619,28 @@ cudaError_t z2_host(bool forward, const float* in_host, float* out_host, const f
                                hc * out_per_h * sizeof(float), cudaMemcpyDefault, c->copy_in));
         return cudaEventRecord(ev_cont[j], c->copy_in);
       };
+      const bool slabs_out = !forward && nslabs > 1;
       auto issue_out = [&](int j) -> cudaError_t {
         const Geom gj = chunk(j);
         const size_t h0 = (size_t)j * Hc, hc = (size_t)gj.H;
-        VP_TRY(cudaStreamWaitEvent(c->copy_out, ev_kern[j], 0));
         float* dst = out_d[j & 1];  // the container's chunk, or stored into
         if (g.accumulate) VP_TRY(cudaStreamWaitEvent(c->copy_out, ev_cont[j], 0));
+        if (slabs_out && j == nchunks - 1) {
+          for (int r = 0; r < nslabs; ++r) {
+            const int lo = scut[r], hi = scut[r + 1];
+            VP_TRY(cudaStreamWaitEvent(c->copy_out, ev_slab[r], 0));
+            VP_TRY(z2_transpose_out_rows(dst, gj, ws[j & 1], lo, hi, g.accumulate ? 1 : 0,
+                                         c->copy_out));
+            *launches += 1;
+            VP_TRY(cudaMemcpy2DAsync(out_host + h0 * out_per_h + (size_t)lo * g.SX,
+                                     out_per_h * sizeof(float), dst + (size_t)lo * g.SX,
+                                     out_per_h * sizeof(float),
+                                     (size_t)(hi - lo) * g.SX * sizeof(float), hc,
+                                     cudaMemcpyDefault, c->copy_out));
+          }
+          return cudaEventRecord(ev_done[j], c->copy_out);
+        }
+        VP_TRY(cudaStreamWaitEvent(c->copy_out, ev_kern[j], 0));
         VP_TRY(z2_transpose_out(forward, dst, gj, ws[j & 1], g.accumulate ? 1 : 0,
                                 c->copy_out));
         VP_TRY(cudaMemcpyAsync(out_host + h0 * out_per_h, dst, hc * out_per_h * sizeof(float),
@@ -587,18 +651,61 @@ cudaError_t z2_host(bool forward, const float* in_host, float* out_host, const f
         const cudaStream_t t = st[k & 1];
         const Geom gk = chunk(k);
         const size_t h0 = (size_t)k * Hc, hc = (size_t)gk.H;
-        // the input slot is free once chunk k - 2 is home (its projection
-        // read it)
-        if (k >= 2) VP_TRY(cudaStreamWaitEvent(c->copy_in, ev_done[k - 2], 0));
-        VP_TRY(cudaMemcpyAsync(in_d[k & 1], in_host + h0 * in_per_h,
-                               hc * in_per_h * sizeof(float), cudaMemcpyDefault, c->copy_in));
-        VP_TRY(cudaEventRecord(ev_in[k], c->copy_in));
-        VP_TRY(cudaStreamWaitEvent(t, ev_in[k], 0));
-        if (k >= 1) VP_TRY(cudaStreamWaitEvent(t, ev_kern[k - 1], 0));  // one at a time
-        if (k >= 2) VP_TRY(cudaStreamWaitEvent(t, ev_done[k - 2], 0));  // workspace free
-        VP_TRY(z2_project(forward, in_d[k & 1], ad, gk, ws[k & 1], t));
+        if (forward && k == 0 && npieces > 1) {
+          // by row pieces: strided copies of rows [lo, hi) of every height,
+          // each transposed and projected (angles whose minor axis is x) on
+          // arrival; then the other angles on blocks of columns
+          float* xt0 = ws[0];
+          float* yt0 = ws[0] + vox * Hp0;
+          for (int p = 0; p < npieces; ++p) {
+            const int lo = cut[p], hi = cut[p + 1];
+            VP_TRY(cudaMemcpy2DAsync(in_d[0] + (size_t)lo * g.SX, vox * sizeof(float),
+                                     in_host + (size_t)lo * g.SX, vox * sizeof(float),
+                                     (size_t)(hi - lo) * g.SX * sizeof(float), hc,
+                                     cudaMemcpyDefault, c->copy_in));
+            VP_TRY(cudaEventRecord(ev_piece[p], c->copy_in));
+            VP_TRY(cudaStreamWaitEvent(t, ev_piece[p], 0));
+            VP_TRY(z2_transpose_in_rows(in_d[0], gk, ws[0], lo, hi, t));
+            *launches += 1;
+            VP_TRY(launch_forward_z0_stream(xt0, yt0, ad, gw, lo, hi, 0, 0, 0, g.n_ang,
+                                            p == 0 ? 0 : 1, t, launches));
+          }
+          VP_TRY(cudaEventRecord(ev_in[k], c->copy_in));
+          VP_TRY(launch_forward_z0_rest(xt0, yt0, ad, gw, t, launches));
+          for (int j = 0; j + 1 < (int)ccut.size(); ++j)
+            VP_TRY(launch_forward_z0_stream(xt0, yt0, ad, gw, 0, 0, ccut[j], ccut[j + 1], 0,
+                                            g.n_ang, 1, t, launches));
+          *launches += 1;  // its transpose back
+        } else {
+          // the input slot is free once chunk k - 2 is home (its projection
+          // read it)
+          if (k >= 2) VP_TRY(cudaStreamWaitEvent(c->copy_in, ev_done[k - 2], 0));
+          VP_TRY(cudaMemcpyAsync(in_d[k & 1], in_host + h0 * in_per_h,
+                                 hc * in_per_h * sizeof(float), cudaMemcpyDefault, c->copy_in));
+          VP_TRY(cudaEventRecord(ev_in[k], c->copy_in));
+          VP_TRY(cudaStreamWaitEvent(t, ev_in[k], 0));
+          if (k >= 1) VP_TRY(cudaStreamWaitEvent(t, ev_kern[k - 1], 0));  // one at a time
+          if (k >= 2) VP_TRY(cudaStreamWaitEvent(t, ev_done[k - 2], 0));  // workspace free
+          if (slabs_out && k == nchunks - 1) {
+            // by row slabs, each handed to the out stream once computed
+            Geom gl = gk;
+            gl.H = gl.Hx = gl.Hy = (int)(((size_t)gk.H + 3) / 4 * 4);
+            gl.accumulate = 0;
+            float* xtl = ws[k & 1];
+            float* ytl = ws[k & 1] + vox * gl.H;
+            VP_TRY(z2_transpose_in(false, in_d[k & 1], gk, ws[k & 1], t));
+            *launches += 1;  // the transposes back are counted per slab
+            for (int r = 0; r < nslabs; ++r) {
+              VP_TRY(launch_backward_z0_rows(ytl, xtl, ad, gl, scut[r], scut[r + 1], t));
+              *launches += launches_backward_z0(ytl, xtl, gl);
+              VP_TRY(cudaEventRecord(ev_slab[r], t));
+            }
+          } else {
+            VP_TRY(z2_project(forward, in_d[k & 1], ad, gk, ws[k & 1], t));
+            *launches += launches_z2(gk, forward);
+          }
+        }
         VP_TRY(cudaEventRecord(ev_kern[k], t));
-        *launches += launches_z2(gk, forward);
         if (k >= 1) {
           VP_TRY(issue_cont(k - 1));
           VP_TRY(issue_out(k - 1));

@@ -133,6 +133,37 @@ cudaError_t z2_transpose_out(bool forward, float* out, const Geom& g, const floa
   return transpose(ws, out, nvox, g.H, Hp, nvox, add, stream);
 }
 
+// The input of the transposed form into ws, in height-fastest order
+// (forward: x -> xt; adjoint: y -> yt), stored.
+cudaError_t z2_transpose_in(bool forward, const float* in, const Geom& g, float* ws,
+                            cudaStream_t stream) {
+  const long long Hp = round4(g.H);
+  const long long nvox = (long long)g.SY * g.SX;
+  const long long nbin = (long long)g.n_ang * g.PX;
+  if (forward) return transpose(in, ws, g.H, nvox, nvox, Hp, 0, stream);
+  return transpose(in, ws + nvox * Hp, g.H, nbin, nbin, Hp, 0, stream);
+}
+
+// Volume rows [lo, hi) of a heights-slowest volume chunk in (g.H, SY, SX)
+// into the transposed form's xt (SY, SX, Hp), stored.
+cudaError_t z2_transpose_in_rows(const float* x, const Geom& g, float* ws, int lo, int hi,
+                                 cudaStream_t stream) {
+  const long long Hp = round4(g.H);
+  const long long nvox = (long long)g.SY * g.SX;
+  return transpose(x + (long long)lo * g.SX, ws + (long long)lo * g.SX * Hp, g.H,
+                   (long long)(hi - lo) * g.SX, nvox, Hp, 0, stream);
+}
+
+// Volume rows [lo, hi) of the adjoint's xt (SY, SX, Hp) in ws into a
+// heights-slowest chunk x (g.H, SY, SX): added (add = 1) or stored (0).
+cudaError_t z2_transpose_out_rows(float* x, const Geom& g, const float* ws, int lo, int hi,
+                                  int add, cudaStream_t stream) {
+  const long long Hp = round4(g.H);
+  const long long nvox = (long long)g.SY * g.SX;
+  return transpose(ws + (long long)lo * g.SX * Hp, x + (long long)lo * g.SX,
+                   (long long)(hi - lo) * g.SX, g.H, Hp, nvox, add, stream);
+}
+
 // x (Hx, SY, SX) -> xt (SY, SX, Hp); yt = A xt; y (Hy, n, PX) += yt^T.
 cudaError_t forward_z2_transposed(const float* x, float* y, const float* angles, const Geom& g,
                                   float* ws, cudaStream_t stream) {

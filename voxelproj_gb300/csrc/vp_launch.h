@@ -52,12 +52,17 @@ cudaError_t z2_transpose_out(bool forward, float* out, const Geom& g, const floa
 // workspace result back into a (g.H, SY, SX) chunk (add = 1 adds, 0 stores).
 // The workspace's z_order 0 views are xt = ws, yt = ws + SY*SX*Hp (Hp = g.H
 // rounded up to 4).
-cudaError_t z2_transpose_in(bool forward, const float* in, const Geom& g, float* ws,
-                            cudaStream_t stream);
 cudaError_t z2_transpose_in_rows(const float* x, const Geom& g, float* ws, int lo, int hi,
                                  cudaStream_t stream);
 cudaError_t z2_transpose_out_rows(float* x, const Geom& g, const float* ws, int lo, int hi,
                                   int add, cudaStream_t stream);
+// Angle ranges likewise: angles [a0, a1) of a (g.H, n_ang, PX) sinogram into
+// the adjoint's workspace (stored), and of the forward's workspace result
+// back into a (g.H, n_ang, PX) sinogram (add = 1 adds, 0 stores).
+cudaError_t z2_transpose_in_angles(const float* y, const Geom& g, float* ws, int a0, int a1,
+                                   cudaStream_t stream);
+cudaError_t z2_transpose_out_angles(float* y, const Geom& g, const float* ws, int a0, int a1,
+                                    int add, cudaStream_t stream);
 
 // Height split of the 8-heights-per-lane forms: heights [0, r8_heights(H))
 // run with 8 per lane (chunks of 256); a last chunk of at most 128 heights

@@ -133,17 +133,6 @@ cudaError_t z2_transpose_out(bool forward, float* out, const Geom& g, const floa
   return transpose(ws, out, nvox, g.H, Hp, nvox, add, stream);
 }
 
-// The input of the transposed form into ws, in height-fastest order
-// (forward: x -> xt; adjoint: y -> yt), stored.
-cudaError_t z2_transpose_in(bool forward, const float* in, const Geom& g, float* ws,
-                            cudaStream_t stream) {
-  const long long Hp = round4(g.H);
-  const long long nvox = (long long)g.SY * g.SX;
-  const long long nbin = (long long)g.n_ang * g.PX;
-  if (forward) return transpose(in, ws, g.H, nvox, nvox, Hp, 0, stream);
-  return transpose(in, ws + nvox * Hp, g.H, nbin, nbin, Hp, 0, stream);
-}
-
 // Volume rows [lo, hi) of a heights-slowest volume chunk in (g.H, SY, SX)
 // into the transposed form's xt (SY, SX, Hp), stored.
 cudaError_t z2_transpose_in_rows(const float* x, const Geom& g, float* ws, int lo, int hi,
@@ -152,6 +141,28 @@ cudaError_t z2_transpose_in_rows(const float* x, const Geom& g, float* ws, int l
   const long long nvox = (long long)g.SY * g.SX;
   return transpose(x + (long long)lo * g.SX, ws + (long long)lo * g.SX * Hp, g.H,
                    (long long)(hi - lo) * g.SX, nvox, Hp, 0, stream);
+}
+
+// Angles [a0, a1) of a heights-slowest sinogram in (g.H, n_ang, PX) into the
+// transposed form's yt (n_ang, PX, Hp), stored.
+cudaError_t z2_transpose_in_angles(const float* y, const Geom& g, float* ws, int a0, int a1,
+                                   cudaStream_t stream) {
+  const long long Hp = round4(g.H);
+  const long long nvox = (long long)g.SY * g.SX;
+  const long long nbin = (long long)g.n_ang * g.PX;
+  return transpose(y + (long long)a0 * g.PX, ws + nvox * Hp + (long long)a0 * g.PX * Hp, g.H,
+                   (long long)(a1 - a0) * g.PX, nbin, Hp, 0, stream);
+}
+
+// Angles [a0, a1) of the forward's yt (n_ang, PX, Hp) in ws into a
+// heights-slowest sinogram y (g.H, n_ang, PX): added (add = 1) or stored (0).
+cudaError_t z2_transpose_out_angles(float* y, const Geom& g, const float* ws, int a0, int a1,
+                                    int add, cudaStream_t stream) {
+  const long long Hp = round4(g.H);
+  const long long nvox = (long long)g.SY * g.SX;
+  const long long nbin = (long long)g.n_ang * g.PX;
+  return transpose(ws + nvox * Hp + (long long)a0 * g.PX * Hp, y + (long long)a0 * g.PX,
+                   (long long)(a1 - a0) * g.PX, g.H, Hp, nbin, add, stream);
 }
 
 // Volume rows [lo, hi) of the adjoint's xt (SY, SX, Hp) in ws into a

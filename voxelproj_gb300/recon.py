@@ -61,16 +61,19 @@ def adam_reconstruct(P: Projector, b: torch.Tensor, steps: int = 50, lr: float =
     vol_shape = (*P.volume_yx, b.shape[2]) if P.z_order == 0 else (b.shape[0], *P.volume_yx)
     x = (x0.clone() if x0 is not None else torch.zeros(vol_shape, device=b.device))
     x.requires_grad_(True)
-    opt = torch.optim.Adam([x], lr=lr)
+    # one fused kernel per update on CUDA
+    opt = torch.optim.Adam([x], lr=lr, fused=x.is_cuda)
     losses = []
     for _ in range(steps):
         opt.zero_grad(set_to_none=True)
-        r = P(x) - b
-        loss = 0.5 * (r.double() ** 2).sum()
+        r = (P(x) - b).reshape(-1)
+        # the gradient of 0.5 r.r with respect to r is r itself; the loss
+        # value is a float32 dot product, kept on the device (no sync per step)
+        loss = 0.5 * torch.dot(r, r)
         loss.backward()
         opt.step()
-        losses.append(float(loss.detach()))
-    return x.detach(), losses
+        losses.append(loss.detach())
+    return x.detach(), [float(v) for v in torch.stack(losses).double().cpu()]
 
 
 def _dot(a: torch.Tensor, b: torch.Tensor) -> torch.Tensor:

@@ -82,7 +82,7 @@ struct BatchDesc {
 };
 
 union BatchSmem {
-  float4 cand[BATCH_WARPS][32 * Fp0Cap<4>::value];
+  float4 cand[BATCH_WARPS][Fp0Cap<4>::list];
   struct {
     RunEntry tab[BATCH_WARPS][BPR_CHUNK];
     int alist[BATCH_WARPS][BPR_LIST];

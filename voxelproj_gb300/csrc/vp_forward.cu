@@ -31,16 +31,18 @@ using namespace detail;
 // vp_fp_z0.cuh).  Blocks of FP0_WARPS warps take neighbouring bin runs of one
 // angle, or with AGROUP one bin run of neighbouring angles; blockIdx.z is the
 // height chunk of 32 * R heights.
+// The 8-height, 4-bin form is held to 7 resident blocks per SM (72
+// registers), its fastest occupancy.
 // With SPLIT a block takes 2 bin runs instead of 4, each by 2 warps that
 // gather half of the slab's major lines each: twice the blocks, each half as
 // long, so the last wave of a launch leaves less of the GPU idle.  The first
 // half writes (in the caller's mode); after a block barrier the second adds.
 template <int R, int KW, bool AGROUP, int UN, bool SPLIT = false>
-__global__ void __launch_bounds__(32 * FP0_WARPS, SPLIT ? (R == 8 ? 7 : 8) : 0)
+__global__ void __launch_bounds__(32 * FP0_WARPS, SPLIT ? (R == 8 ? 7 : 8) : (R == 8 && KW == 4 ? 7 : 0))
     fp_z0_kernel(const float* __restrict__ x, float* __restrict__ y,
                  const float* __restrict__ angles, Geom g, int a_base, Slab slab,
                  int accumulate) {
-  __shared__ float4 cand[FP0_WARPS][32 * Fp0Cap<KW>::value];
+  __shared__ float4 cand[FP0_WARPS][Fp0Cap<KW>::list];
   const int lane = threadIdx.x;
   const int w = threadIdx.y;
   const int h = blockIdx.z * 32 * R + lane * (R == 8 ? 4 : R);

@@ -61,8 +61,12 @@ constexpr int FP0_UNROLL = 4;  // candidates whose loads are in flight together 
 template <int KW>
 struct Fp0Cap {
   static constexpr int value = KW == 4 ? 10 : 15;
+  // a warp's list: 32 lines of candidates, then padding for the loads of the
+  // last group of FP0_UNROLL
+  static constexpr int list = 32 * value + 4;
   static_assert(KW == 4 || KW == 8, "bins per warp: 4 or 8");
   static_assert(KW + 1 < (1 << FP0_QBITS), "q must fit its bits");
+  static_assert(FP0_UNROLL <= 4, "list padding");
 };
 
 // Adds a candidate's weights to the run's accumulators: bin q-2 gets w0, q-1
@@ -120,7 +124,7 @@ __host__ __device__ inline Slab slab_of(int k, bool cls, int wy, int wx, int SY,
 // One warp: angle a, bins [p0, p0 + KW), this lane's heights from h (LaneH:
 // R = 8 is [h, h + 4) and [h + 128, h + 132)), the voxels of slab s.
 // UN candidates are loaded together.  cand is this warp's shared candidate list of
-// 32 * Fp0Cap<KW>::value entries.  All 32 lanes must call it together.
+// Fp0Cap<KW>::list entries.  All 32 lanes must call it together.
 // wait() runs (by the whole warp) just before the outputs are written; with
 // Wait::coherent the read of the output bypasses L1.
 template <int R, int KW, int UN = FP0_UNROLL, class Wait = NoWait>
@@ -194,13 +198,16 @@ __device__ __forceinline__ void fp_z0_warp(const float* __restrict__ x, float* _
       e.w = __int_as_float((vox << FP0_QBITS) | q);
       cand[start + t] = e;
     }
+    // padding after the list: voxel 0 with zero weights, so that the last
+    // group's loads need no condition (its extra entries are not added)
+    if (lane < UN) cand[total + lane] = make_float4(0.f, 0.f, 0.f, 0.f);
     __syncwarp();
     for (int c0 = 0; c0 < total; c0 += UN) {
       float4 e[UN];
       V xv[UN];
 #pragma unroll
       for (int u = 0; u < UN; ++u) {
-        e[u] = (c0 + u < total) ? cand[c0 + u] : make_float4(0.f, 0.f, 0.f, 0.f);
+        e[u] = cand[c0 + u];
         const int vox = __float_as_int(e[u].w) >> FP0_QBITS;
         xv[u] = lh.load(xs + (size_t)vox * g.Hx);
       }

@@ -84,6 +84,8 @@ __device__ __forceinline__ void scatter_q(V (&acc)[KW], const float4& e, const V
   case Q:                                                       \
     if constexpr (Q <= KW + 1) scatter3<KW, Q>(acc, e, xv);     \
     break;
+  // the list builder clamps q to [0, KW + 1]: no range check needed
+  __builtin_assume(q >= 0 && q <= KW + 1);
   switch (q) {
     VP_Q_CASE(0) VP_Q_CASE(1) VP_Q_CASE(2) VP_Q_CASE(3) VP_Q_CASE(4)
     VP_Q_CASE(5) VP_Q_CASE(6) VP_Q_CASE(7) VP_Q_CASE(8) VP_Q_CASE(9)

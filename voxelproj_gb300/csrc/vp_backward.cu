@@ -157,7 +157,7 @@ __global__ void __launch_bounds__(32 * BPB_WARPS)
 // saw no angle of its class leaves x untouched (in store mode the first launch
 // always writes).
 // ---------------------------------------------------------------------------
-template <int PASS, int R, bool ADD = false>
+template <int PASS, int R, bool ADD = false, bool FULL = false>
 __global__ void __launch_bounds__(32 * BPR_WARPS, R == 8 ? 5 : 0)
     bp_z0_runs_kernel(const float* __restrict__ y, float* __restrict__ x,
                       const float* __restrict__ angles, Geom g, int nrun_major, int run_base,
@@ -172,8 +172,9 @@ __global__ void __launch_bounds__(32 * BPR_WARPS, R == 8 ? 5 : 0)
   int xi0, yi0;
   run_origin<PASS>(run, nrun_major, &xi0, &yi0);
   if (yi0 >= row_end) return;
-  bp_runs_warp<PASS, R, NoWait, ADD>(y, x, angles, g, xi0, yi0, blockIdx.y * 32 * R + lane * 4,
-                                     accumulate, tab[w], alist[w], NoWait(), addend);
+  bp_runs_warp<PASS, R, NoWait, ADD, FULL>(y, x, angles, g, xi0, yi0,
+                                           blockIdx.y * 32 * R + lane * 4, accumulate, tab[w],
+                                           alist[w], NoWait(), addend);
 }
 
 // Bounded-wait timeouts of this library's kernels (0 in correct operation).
@@ -398,10 +399,10 @@ cudaError_t launch_bp_z0_runs_tma(const float* y, float* x, const float* angles,
 // multiple of RUN (class-1 runs span RUN rows).
 // With addend, the class-1 launch also adds addend (same layout as x) into the
 // rows it writes, after its own sums: x = (x + A^T y) + addend.
-template <int R>
-cudaError_t launch_bp_z0_runs(const float* y, float* x, const float* angles, const Geom& g,
-                              int row_lo, int row_hi, cudaStream_t stream,
-                              const float* addend = nullptr) {
+template <int R, bool FULL = false>
+cudaError_t launch_bp_z0_runs_h(const float* y, float* x, const float* angles, const Geom& g,
+                                int row_lo, int row_hi, cudaStream_t stream,
+                                const float* addend = nullptr) {
   dim3 block(32, BPR_WARPS);
   const unsigned hchunks = ceil_div(g.H, 32 * R);
   const int nmaj0 = (int)ceil_div(g.SX, RUN);
@@ -409,7 +410,8 @@ cudaError_t launch_bp_z0_runs(const float* y, float* x, const float* angles, con
   const long long b0 = (long long)row_lo * nmaj0;
   const long long e0 = (long long)ceil_div(row_hi, RUN) * RUN * nmaj0;
   if (e0 > b0) {
-    bp_z0_runs_kernel<0, R><<<dim3(ceil_div(e0 - b0, BPR_WARPS), hchunks), block, 0, stream>>>(
+    bp_z0_runs_kernel<0, R, false, FULL><<<dim3(ceil_div(e0 - b0, BPR_WARPS), hchunks), block, 0,
+                                            stream>>>(
         y, x, angles, g, nmaj0, (int)b0, (int)e0, row_hi, g.accumulate);
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
@@ -419,14 +421,25 @@ cudaError_t launch_bp_z0_runs(const float* y, float* x, const float* angles, con
   if (e1 > b1) {
     const dim3 grid(ceil_div(e1 - b1, BPR_WARPS), hchunks);
     if (addend)
-      bp_z0_runs_kernel<1, R, true><<<grid, block, 0, stream>>>(
+      bp_z0_runs_kernel<1, R, true, FULL><<<grid, block, 0, stream>>>(
           y, x, angles, g, g.SX, (int)b1, (int)e1, row_hi, 1, addend);
     else
-      bp_z0_runs_kernel<1, R><<<grid, block, 0, stream>>>(y, x, angles, g, g.SX, (int)b1,
-                                                          (int)e1, row_hi, 1);
+      bp_z0_runs_kernel<1, R, false, FULL><<<grid, block, 0, stream>>>(
+          y, x, angles, g, g.SX, (int)b1, (int)e1, row_hi, 1);
     return cudaGetLastError();
   }
   return cudaSuccess;
+}
+
+// The run launches, with the constant-offset loads when every lane's heights
+// are inside [0, H) (8 per lane and whole chunks of 256).
+template <int R>
+cudaError_t launch_bp_z0_runs(const float* y, float* x, const float* angles, const Geom& g,
+                              int row_lo, int row_hi, cudaStream_t stream,
+                              const float* addend = nullptr) {
+  if (R == 8 && g.H % (32 * 8) == 0)
+    return launch_bp_z0_runs_h<R, true>(y, x, angles, g, row_lo, row_hi, stream, addend);
+  return launch_bp_z0_runs_h<R, false>(y, x, angles, g, row_lo, row_hi, stream, addend);
 }
 
 // Runs with 8 heights per lane on heights [0, r8_heights(H)) and 4 on the

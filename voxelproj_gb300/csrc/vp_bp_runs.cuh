@@ -29,7 +29,7 @@ struct RunEntry {
 // then applies the four voxels' weights.
 // p points at the window's first bin at this lane's first height (lh.s0);
 // stride is the signed distance between consecutive window bins.
-template <int PAT, int R>
+template <int PAT, int R, bool FULL = false>
 __device__ __forceinline__ void run_window(typename Vec<R>::T (&acc)[RUN], const float4 (&wv)[3],
                                            const float* p, ptrdiff_t stride, const LaneH<R>& lh) {
   constexpr int o1 = (PAT & 1);
@@ -38,7 +38,7 @@ __device__ __forceinline__ void run_window(typename Vec<R>::T (&acc)[RUN], const
   constexpr int W = 3 + o3;
   typename Vec<R>::T win[W];
 #pragma unroll
-  for (int u = 0; u < W; ++u) win[u] = lh.load(p + u * stride);
+  for (int u = 0; u < W; ++u) win[u] = lh.template load<FULL>(p + u * stride);
   const float ws[12] = {wv[0].x, wv[0].y, wv[0].z, wv[0].w, wv[1].x, wv[1].y,
                         wv[1].z, wv[1].w, wv[2].x, wv[2].y, wv[2].z, wv[2].w};
   constexpr int off[RUN] = {0, o1, o2, o3};
@@ -148,12 +148,13 @@ __device__ __forceinline__ RunEntry run_entry(const float* angles, int a, const 
 }
 
 // One warp: the run of class PASS starting at voxel (xi0, yi0), this lane's
-// heights from h (R = 4: [h, h + 4); R = 8: also [h + 128, h + 132)).  tab
+// heights from h (R = 4: [h, h + 4); R = 8: also [h + 128, h + 132); FULL:
+// all of them inside [0, H)).  tab
 // (BPR_CHUNK entries) and alist (BPR_LIST ints) are this warp's shared
 // tables.  All 32 lanes must call it together.  wait() runs (by the whole
 // warp) just before the outputs are written; with Wait::coherent the read of
 // the output bypasses L1.
-template <int PASS, int R = 4, class Wait = NoWait, bool ADD = false>
+template <int PASS, int R = 4, class Wait = NoWait, bool ADD = false, bool FULL = false>
 __device__ __forceinline__ void bp_runs_warp(const float* __restrict__ y, float* __restrict__ x,
                                              const float* __restrict__ angles, const Geom& g,
                                              int xi0, int yi0, int h, int accumulate,
@@ -191,14 +192,14 @@ __device__ __forceinline__ void bp_runs_warp(const float* __restrict__ y, float*
         const float* p = y + off + lh.s0;
         const ptrdiff_t stride = meta.z;
         switch (meta.w) {
-          case 0: run_window<0, R>(acc, wv, p, stride, lh); break;
-          case 1: run_window<1, R>(acc, wv, p, stride, lh); break;
-          case 2: run_window<2, R>(acc, wv, p, stride, lh); break;
-          case 3: run_window<3, R>(acc, wv, p, stride, lh); break;
-          case 4: run_window<4, R>(acc, wv, p, stride, lh); break;
-          case 5: run_window<5, R>(acc, wv, p, stride, lh); break;
-          case 6: run_window<6, R>(acc, wv, p, stride, lh); break;
-          case 7: run_window<7, R>(acc, wv, p, stride, lh); break;
+          case 0: run_window<0, R, FULL>(acc, wv, p, stride, lh); break;
+          case 1: run_window<1, R, FULL>(acc, wv, p, stride, lh); break;
+          case 2: run_window<2, R, FULL>(acc, wv, p, stride, lh); break;
+          case 3: run_window<3, R, FULL>(acc, wv, p, stride, lh); break;
+          case 4: run_window<4, R, FULL>(acc, wv, p, stride, lh); break;
+          case 5: run_window<5, R, FULL>(acc, wv, p, stride, lh); break;
+          case 6: run_window<6, R, FULL>(acc, wv, p, stride, lh); break;
+          case 7: run_window<7, R, FULL>(acc, wv, p, stride, lh); break;
           case BPR_SKIP: break;
           default: {
             // generic path: three guarded loads per voxel, bins relative to
@@ -214,7 +215,7 @@ __device__ __forceinline__ void bp_runs_warp(const float* __restrict__ y, float*
               for (int kk = 0; kk < 3; ++kk) {
                 const int bin = rr[m] + dir * (kk - 1);
                 const V v = (unsigned)bin < (unsigned)g.PX
-                                ? lh.load(p + (ptrdiff_t)(bin - base) * g.Hy)
+                                ? lh.template load<FULL>(p + (ptrdiff_t)(bin - base) * g.Hy)
                                 : vzero<V>();
                 acc[m] = f4_fma(ws[3 * m + kk], v, acc[m]);
               }

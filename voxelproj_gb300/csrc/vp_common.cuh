@@ -228,12 +228,15 @@ struct LaneH {
       d[k] = (v[k] ? h + k * kSecondHalf : 0) - s0;
     }
   }
-  // this lane's heights of a row, given q = row + s0
+  // this lane's heights of a row, given q = row + s0.  FULL: every lane's
+  // heights are inside [0, H) (whole chunks), so the second float4 is at the
+  // constant offset kSecondHalf.
+  template <bool FULL = false>
   __device__ __forceinline__ typename Vec<R>::T load(const float* q) const {
     if constexpr (R == 8) {
       float4x2 r;
       r.a = __ldg(reinterpret_cast<const float4*>(q));
-      r.b = __ldg(reinterpret_cast<const float4*>(q + d[1]));
+      r.b = __ldg(reinterpret_cast<const float4*>(q + (FULL ? kSecondHalf : d[1])));
       return r;
     } else {
       return __ldg(reinterpret_cast<const typename Vec<R>::T*>(q));

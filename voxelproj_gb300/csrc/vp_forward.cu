@@ -37,7 +37,7 @@ using namespace detail;
 // gather half of the slab's major lines each: twice the blocks, each half as
 // long, so the last wave of a launch leaves less of the GPU idle.  The first
 // half writes (in the caller's mode); after a block barrier the second adds.
-template <int R, int KW, bool AGROUP, int UN, bool SPLIT = false>
+template <int R, int KW, bool AGROUP, int UN, bool SPLIT = false, bool FULL = false>
 __global__ void __launch_bounds__(32 * FP0_WARPS, SPLIT ? (R == 8 ? 7 : 8) : (R == 8 && KW == 4 ? 7 : 0))
     fp_z0_kernel(const float* __restrict__ x, float* __restrict__ y,
                  const float* __restrict__ angles, Geom g, int a_base, Slab slab,
@@ -61,7 +61,7 @@ __global__ void __launch_bounds__(32 * FP0_WARPS, SPLIT ? (R == 8 ? 7 : 8) : (R 
   } else {
     const int p0 = (AGROUP ? blockIdx.x : blockIdx.x * FP0_WARPS + w) * KW;
     const int a = a_base + (AGROUP ? blockIdx.y * FP0_WARPS + w : blockIdx.y);
-    fp_z0_warp<R, KW, UN>(x, y, angles, g, p0, a, h, slab, accumulate, cand[w]);
+    fp_z0_warp<R, KW, UN, NoWait, FULL>(x, y, angles, g, p0, a, h, slab, accumulate, cand[w]);
   }
 }
 
@@ -250,7 +250,7 @@ struct SlabLaunch {
   int a_lo, a_hi;
 };
 
-template <int R, int KW, bool AGROUP, int UN, bool SPLIT = false>
+template <int R, int KW, bool AGROUP, int UN, bool SPLIT = false, bool FULL = false>
 cudaError_t launch_slab(const SlabLaunch& L, cudaStream_t stream, int* launches) {
   dim3 block(32, FP0_WARPS);
   const long long per_launch = AGROUP ? (long long)kMaxGridYZ * FP0_WARPS : kMaxGridYZ;
@@ -263,7 +263,7 @@ cudaError_t launch_slab(const SlabLaunch& L, cudaStream_t stream, int* launches)
                                 : ceil_div(g.PX, KW * FP0_WARPS);
     const unsigned gy = AGROUP ? ceil_div(na, FP0_WARPS) : (unsigned)na;
     dim3 grid(gx, gy, ceil_div(g.H, 32 * R));
-    fp_z0_kernel<R, KW, AGROUP, UN, SPLIT><<<grid, block, 0, stream>>>(L.x, L.y, L.angles, g,
+    fp_z0_kernel<R, KW, AGROUP, UN, SPLIT, FULL><<<grid, block, 0, stream>>>(L.x, L.y, L.angles, g,
                                                                 (int)a_base, L.slab,
                                                                 L.accumulate);
     if (launches) ++*launches;
@@ -288,6 +288,8 @@ cudaError_t launch_slab_config(const Fp0Config& c, const SlabLaunch& L, cudaStre
     if (c.KW == 8) return launch_slab<8, 8, false, 2>(L, s, n);
     if (c.un == 2) {
       if (c.split) return launch_slab<8, 4, false, 2, true>(L, s, n);
+      // whole chunks of 256 heights: the second float4 at a constant offset
+      if (L.g.H % (32 * 8) == 0) return launch_slab<8, 4, false, 2, false, true>(L, s, n);
       return launch_slab<8, 4, false, 2>(L, s, n);
     }
     return launch_slab<8, 4, false, 4>(L, s, n);

@@ -124,12 +124,13 @@ __host__ __device__ inline Slab slab_of(int k, bool cls, int wy, int wx, int SY,
 }
 
 // One warp: angle a, bins [p0, p0 + KW), this lane's heights from h (LaneH:
-// R = 8 is [h, h + 4) and [h + 128, h + 132)), the voxels of slab s.
+// R = 8 is [h, h + 4) and [h + 128, h + 132)), the voxels of slab s.  FULL:
+// every lane's heights are inside [0, H).
 // UN candidates are loaded together.  cand is this warp's shared candidate list of
 // Fp0Cap<KW>::list entries.  All 32 lanes must call it together.
 // wait() runs (by the whole warp) just before the outputs are written; with
 // Wait::coherent the read of the output bypasses L1.
-template <int R, int KW, int UN = FP0_UNROLL, class Wait = NoWait>
+template <int R, int KW, int UN = FP0_UNROLL, class Wait = NoWait, bool FULL = false>
 __device__ __forceinline__ void fp_z0_warp(const float* __restrict__ x, float* __restrict__ y,
                                            const float* __restrict__ angles, const Geom& g,
                                            int p0, int a, int h, const Slab& s,
@@ -211,7 +212,7 @@ __device__ __forceinline__ void fp_z0_warp(const float* __restrict__ x, float* _
       for (int u = 0; u < UN; ++u) {
         e[u] = cand[c0 + u];
         const int vox = __float_as_int(e[u].w) >> FP0_QBITS;
-        xv[u] = lh.load(xs + (size_t)vox * g.Hx);
+        xv[u] = lh.template load<FULL>(xs + (size_t)vox * g.Hx);
       }
 #pragma unroll
       for (int u = 0; u < UN; ++u) {

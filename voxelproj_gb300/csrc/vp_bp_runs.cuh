@@ -191,6 +191,8 @@ __device__ __forceinline__ void bp_runs_warp(const float* __restrict__ y, float*
             (long long)(unsigned)meta.x | ((long long)meta.y << 32);
         const float* p = y + off + lh.s0;
         const ptrdiff_t stride = meta.z;
+        // run_entry writes a pattern, BPR_GENERIC or BPR_SKIP
+        __builtin_assume(meta.w >= 0 && meta.w <= BPR_SKIP);
         switch (meta.w) {
           case 0: run_window<0, R, FULL>(acc, wv, p, stride, lh); break;
           case 1: run_window<1, R, FULL>(acc, wv, p, stride, lh); break;

@@ -45,7 +45,6 @@
 
 #include <cmath>
 #include <cstdint>
-#include <cstdlib>
 #include <mutex>
 #include <vector>
 

@@ -173,6 +173,7 @@ __device__ __forceinline__ void bp_runs_warp(const float* __restrict__ y, float*
   for (int m = 0; m < RUN; ++m) acc[m] = vzero<V>();
 
   int seen = 0;
+  const float* ys = y + lh.s0;  // this lane's heights of bin 0 of angle 0
 
   for (int w0 = 0; w0 < g.n_ang; w0 += BPR_LIST) {
     // this warp's list of the class's angles in [w0, w0 + BPR_LIST), ascending
@@ -189,7 +190,7 @@ __device__ __forceinline__ void bp_runs_warp(const float* __restrict__ y, float*
         const float4 wv[3] = {e.w[0], e.w[1], e.w[2]};
         const long long off =
             (long long)(unsigned)meta.x | ((long long)meta.y << 32);
-        const float* p = y + off + lh.s0;
+        const float* p = ys + off;
         const ptrdiff_t stride = meta.z;
         // run_entry writes a pattern, BPR_GENERIC or BPR_SKIP
         __builtin_assume(meta.w >= 0 && meta.w <= BPR_SKIP);

@@ -43,6 +43,26 @@ def test_weights_are_voxel_area_per_bin(phi, xp):
     assert abs(w.sum() - 1.0) < 1e-14
 
 
+@pytest.mark.parametrize("phi", [0.0, 0.3, np.pi / 4, 1.0, np.pi / 2, 2.0, 3 * np.pi / 4, -1.2,
+                                 5.5, 15.0])
+def test_angle_params_trapezoid(phi):
+    """Per-angle constants (sp_backward_z0.cuh:45-58): the unit square's
+    footprint at angle phi is a trapezoid with plateau half-width a and foot
+    half-width b, the two values |c -+ s| / 2 in increasing order, and height
+    ymax = 1 / (a + b), so that its area is one."""
+    k = oracle.angle_params(phi)
+    p = np.float64(np.float32(phi))
+    c, s = np.cos(p), np.sin(p)
+    np.testing.assert_allclose([k["c"], k["s"]], [c, s], rtol=0, atol=1e-15)
+    half = sorted([abs(c - s) / 2, abs(c + s) / 2])
+    np.testing.assert_allclose([k["a"], k["b"]], half, rtol=0, atol=1e-15)
+    assert 0.0 <= k["a"] <= k["b"]
+    np.testing.assert_allclose(k["ymax"] * (k["a"] + k["b"]), 1.0, rtol=1e-15)
+    # a + b = max(|c|, |s|): the footprint's foot is as wide as the square's
+    # longer projected side
+    np.testing.assert_allclose(k["a"] + k["b"], max(abs(c), abs(s)), rtol=1e-15)
+
+
 def test_weights_closed_forms():
     # phi = 0: box of width 1 -> all weight in the nearest bin at integer xp
     r, w = oracle.weights(0.0, 7.0)

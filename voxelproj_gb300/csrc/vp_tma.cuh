@@ -85,14 +85,5 @@ __device__ __forceinline__ void tensor3d_g2s(void* dst, const CUtensorMap* map, 
       : "memory");
 }
 
-// Bulk copy of `bytes` from global src to shared dst, completing on bar.
-__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned bytes,
-                                         uint64_t* bar) {
-  asm volatile(
-      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
-      ::"r"(smem_addr(dst)), "l"(src), "r"(bytes), "r"(smem_addr(bar))
-      : "memory");
-}
-
 }  // namespace tma
 }  // namespace vp

@@ -161,8 +161,9 @@ VP_API int vp_forward_z2_noalloc(const float* x, int64_t x0, int64_t x1, int64_t
 /* ---- Batches -----------------------------------------------------------
  * Many problems of different sizes and angle counts, forward and adjoint
  * mixed, in one persistent kernel launch per body present: the forward and
- * the run adjoint with 4 or 8 heights per lane, so at most four launches
- * however many problems.  Each body keeps its single-problem kernel's
+ * the run adjoint with 4 or 8 heights per lane, the 8-height forms in two
+ * bodies (whole 256-height chunks or not), so at most six launches however
+ * many problems.  Each body keeps its single-problem kernel's
  * register budget.  No counterpart in the reference, which launches one
  * kernel per call.
  *

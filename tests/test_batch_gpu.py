@@ -72,8 +72,9 @@ def test_batch_matches_single_problem_calls(vf, vb):
 
 def test_batch_stages_on_large_problems():
     """Problems with several volume slabs (forward stages) and both angle
-    classes (adjoint stages) in one launch, 8 heights per lane with a
-    half-filled second height chunk, against single-problem calls."""
+    classes (adjoint stages) in one launch, 8 heights per lane on a whole
+    256-height chunk (the constant-offset bodies) and a 4-height part for the
+    last 4 heights, against single-problem calls."""
     probs, refs = [], []
     for side, n in [(320, 60), (200, 45), (96, 30)]:
         a = torch.linspace(0, np.pi, n + 1, device="cuda")[:-1].contiguous()
@@ -125,10 +126,11 @@ def test_batch_graph_replays_accumulate():
 
 
 def test_batch_launches_one_kernel_per_body():
-    """Problems of both directions and both height forms: one persistent
-    launch per body, four in all for any number of problems."""
+    """Problems of both directions and all height forms (4 per lane; 8 per
+    lane on a part of whole 256-height chunks; 8 per lane on 200 heights):
+    one persistent launch per body, six in all for any number of problems."""
     probs = []
-    for side, H in [(40, 64), (36, 260), (48, 96), (30, 264)]:
+    for side, H in [(40, 64), (36, 260), (48, 96), (30, 264), (28, 200)]:
         a = torch.linspace(0, np.pi, 20, device="cuda")
         x = torch.randn(side, side, H, device="cuda")
         y = torch.randn(20, side, H, device="cuda")
@@ -137,7 +139,7 @@ def test_batch_launches_one_kernel_per_body():
     before = _lib.LIB.vp_launch_count()
     b.run()
     torch.cuda.synchronize()
-    assert _lib.LIB.vp_launch_count() - before == 4
+    assert _lib.LIB.vp_launch_count() - before == 6
     assert not b.error()
     b.close()
 

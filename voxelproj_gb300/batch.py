@@ -1,7 +1,7 @@
 """Batched projections in persistent launches, replayable as a CUDA graph.
 
     b = Batch([("forward", x1, y1, angles1), ("backward", y2, x2, angles2, 4), ...])
-    b.run()                 # one persistent launch per body present (at most 4)
+    b.run()                 # one persistent launch per body present (at most 6)
     g = b.graph()           # CUDA graph of the same launches
     g.replay()
 

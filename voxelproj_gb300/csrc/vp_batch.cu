@@ -1,11 +1,11 @@
 // Batched projections: many problems of different sizes and angle counts,
-// A and A^T mixed, in one persistent launch per body (at most four).
+// A and A^T mixed, in one persistent launch per body (at most six).
 //
 // vp_batch_create validates the problems, splits each into work items and
 // uploads a descriptor table (the only allocations: the table, the stage
 // counters and an error flag).  vp_batch_run resets the counters and, for
-// each body present (forward or run adjoint, 4 or 8 heights per lane),
-// launches one persistent kernel with a full wave of blocks (SMs x resident
+// each body present (forward or run adjoint, 4 or 8 heights per lane, the
+// 8-height forms also on whole 256-height chunks), launches one persistent kernel with a full wave of blocks (SMs x resident
 // blocks).
 // Each block repeatedly takes the next item from a global counter, finds its
 // problem by binary search and runs the same per-warp bodies, with the same
@@ -142,7 +142,8 @@ __device__ __forceinline__ void signal_done(unsigned* counter) {
 // A forward item's outputs are the bins of one (height chunk, angle, bin
 // group) tile, written by one item per stage; its counter counts the warps
 // done on the tile, so a stage waits for the tile's previous stage alone.
-template <int R>
+// FULL: the part's heights are whole 256-height chunks (R = 8).
+template <int R, bool FULL>
 __device__ __forceinline__ void run_fwd_item(const BatchDesc& d, int stage, int in_stage,
                                              int hc, BatchSmem& sm, WaitSlot* slot, int w,
                                              int lane, unsigned* counters, int* error) {
@@ -156,12 +157,13 @@ __device__ __forceinline__ void run_fwd_item(const BatchDesc& d, int stage, int 
   __syncwarp();
   const int p0 = (bg * BATCH_WARPS + w) * 4;
   const int h = hc * 32 * R + lane * 4;
-  fp_z0_warp<R, 4, UN>(d.in, d.out, d.angles, d.g, p0, a, h, slab, 1, sm.cand[w],
-                       SlotWait{slot});
+  fp_z0_warp<R, 4, UN, SlotWait, FULL>(d.in, d.out, d.angles, d.g, p0, a, h, slab, 1,
+                                       sm.cand[w], SlotWait{slot});
   signal_done(slot->counter);
 }
 
-template <int R>
+// FULL: the part's heights are whole 256-height chunks (R = 8).
+template <int R, bool FULL>
 __device__ __forceinline__ void run_bwd_runs_item(const BatchDesc& d, int stage, int grp,
                                                   int hc, BatchSmem& sm, int w, int lane,
                                                   unsigned* counters, int* error) {
@@ -172,35 +174,43 @@ __device__ __forceinline__ void run_bwd_runs_item(const BatchDesc& d, int stage,
     int xi0, yi0;
     run_origin<0>(run, (d.g.SX + RUN - 1) / RUN, &xi0, &yi0);
     if (run < d.nruns0 && yi0 < d.g.SY)
-      bp_runs_warp<0, R>(d.in, d.out, d.angles, d.g, xi0, yi0, h, 1, sm.runs.tab[w],
-                         sm.runs.alist[w]);
+      bp_runs_warp<0, R, NoWait, false, FULL>(d.in, d.out, d.angles, d.g, xi0, yi0, h, 1,
+                                              sm.runs.tab[w], sm.runs.alist[w]);
   } else if (run < d.nruns1) {
     const StageWait wt{ctr - 1, (unsigned)(d.groups0 * BATCH_WARPS), error};
-    bp_runs_warp<1, R>(d.in, d.out, d.angles, d.g, run % d.g.SX, (run / d.g.SX) * RUN, h, 1,
-                       sm.runs.tab[w], sm.runs.alist[w], wt);
+    bp_runs_warp<1, R, StageWait, false, FULL>(d.in, d.out, d.angles, d.g, run % d.g.SX,
+                                               (run / d.g.SX) * RUN, h, 1, sm.runs.tab[w],
+                                               sm.runs.alist[w], wt);
   }
   signal_done(ctr);
 }
 
 // One kernel instance per body: the forward or the run adjoint with 4 or 8
-// heights per lane (the 2x2 block adjoint rides with the 4-height adjoint).
+// heights per lane (the 2x2 block adjoint rides with the 4-height adjoint),
+// and the 8-height forms again for parts of whole 256-height chunks, whose
+// second float4 is at a constant offset (FWD8F, BWD8F), as in the
+// single-problem launches.
 // Each instance gets the register allocation of its single-problem kernel, so
 // no body runs at another body's occupancy; a plan launches the instances of
 // the bodies it holds, one persistent launch each.
-constexpr int B_FWD4 = 0, B_FWD8 = 1, B_BWD4 = 2, B_BWD8 = 3, NBODIES = 4;
+constexpr int B_FWD4 = 0, B_FWD8 = 1, B_BWD4 = 2, B_BWD8 = 3, B_FWD8F = 4, B_BWD8F = 5,
+              NBODIES = 6;
 
 __host__ __device__ inline int body_of(const BatchDesc& d) {
-  if (d.kind == K_FWD) return d.R == 8 ? B_FWD8 : B_FWD4;
-  return (d.kind == K_BWD_RUNS && d.R == 8) ? B_BWD8 : B_BWD4;
+  if (d.kind == K_FWD) return d.R == 8 ? (d.g.H % 256 == 0 ? B_FWD8F : B_FWD8) : B_FWD4;
+  if (d.kind == K_BWD_RUNS && d.R == 8) return d.g.H % 256 == 0 ? B_BWD8F : B_BWD8;
+  return B_BWD4;
 }
 
 // Resident blocks per SM the registers must allow, so that each body keeps
 // its single-problem kernel's occupancy despite the item bookkeeping:
-// 8-height forward 7 (72 registers, a few spilled; at 6 blocks the 64-cube
+// 8-height forwards 7 (72 registers, a few spilled; at 6 blocks the 64-cube
 // batch took 332 ms instead of 322), 4-height forward 7 (72), 8-height run
-// adjoint 5 (96); the 4-height adjoints as the compiler chooses (72).
+// adjoints 5 (96); the 4-height adjoints as the compiler chooses (72).
 constexpr int batch_min_blocks(int body) {
-  return body == B_FWD8 ? 7 : body == B_FWD4 ? 7 : body == B_BWD8 ? 5 : 0;
+  return (body == B_FWD8 || body == B_FWD8F || body == B_FWD4) ? 7
+         : (body == B_BWD8 || body == B_BWD8F)                  ? 5
+                                                                : 0;
 }
 
 template <int BODY>
@@ -231,17 +241,18 @@ __global__ void __launch_bounds__(BATCH_THREADS, batch_min_blocks(BODY))
     const int local = (int)(item - d.begin);
     const int hc = local / (int)d.per_chunk;
     const int in_chunk = local - hc * (int)d.per_chunk;
-    if constexpr (BODY == B_FWD4 || BODY == B_FWD8) {
-      constexpr int R = BODY == B_FWD8 ? 8 : 4;
+    if constexpr (BODY == B_FWD4 || BODY == B_FWD8 || BODY == B_FWD8F) {
+      constexpr int R = BODY == B_FWD4 ? 4 : 8;
       const int per_stage = d.g.n_ang * d.units;
       const int stage = in_chunk / per_stage;
-      run_fwd_item<R>(d, stage, in_chunk - stage * per_stage, hc, sm, &slots[w], w, lane,
-                      counters, error);
-    } else if (BODY == B_BWD8 || d.kind == K_BWD_RUNS) {
-      constexpr int R = BODY == B_BWD8 ? 8 : 4;
+      run_fwd_item<R, BODY == B_FWD8F>(d, stage, in_chunk - stage * per_stage, hc, sm,
+                                       &slots[w], w, lane, counters, error);
+    } else if (BODY == B_BWD8 || BODY == B_BWD8F || d.kind == K_BWD_RUNS) {
+      constexpr int R = (BODY == B_BWD8 || BODY == B_BWD8F) ? 8 : 4;
       const bool first = in_chunk < d.groups0;
-      run_bwd_runs_item<R>(d, first ? 0 : 1, first ? in_chunk : in_chunk - d.groups0, hc, sm,
-                           w, lane, counters, error);
+      run_bwd_runs_item<R, BODY == B_BWD8F>(d, first ? 0 : 1,
+                                            first ? in_chunk : in_chunk - d.groups0, hc, sm, w,
+                                            lane, counters, error);
     } else {
       const int bidx = in_chunk * BATCH_WARPS + w;
       if (bidx < d.nblocks)
@@ -260,7 +271,8 @@ using BatchKernelFn = void (*)(const BatchDesc*, int, long long, unsigned long l
 
 const void* batch_kernel_for(int body) {
   static const BatchKernelFn fns[NBODIES] = {batch_kernel<B_FWD4>, batch_kernel<B_FWD8>,
-                                             batch_kernel<B_BWD4>, batch_kernel<B_BWD8>};
+                                             batch_kernel<B_BWD4>, batch_kernel<B_BWD8>,
+                                             batch_kernel<B_FWD8F>, batch_kernel<B_BWD8F>};
   return reinterpret_cast<const void*>(fns[body]);
 }
 

@@ -163,9 +163,9 @@ VP_API int vp_forward_z2_noalloc(const float* x, int64_t x0, int64_t x1, int64_t
  * mixed, in one persistent kernel launch per body present: the forward and
  * the run adjoint with 4 or 8 heights per lane, the 8-height forms in two
  * bodies (whole 256-height chunks or not), so at most six launches however
- * many problems.  Each body keeps its single-problem kernel's
- * register budget.  No counterpart in the reference, which launches one
- * kernel per call.
+ * many problems.  Each body keeps its single-problem kernel's register
+ * budget.  No counterpart in the reference, which launches one kernel per
+ * call.
  *
  * A problem is in z_order 0 layout (x (SY, SX, H), y (n_ang, PX, H)) with
  * heights a multiple of 4 and 16-byte aligned buffers; its output is

@@ -156,12 +156,14 @@ __device__ __forceinline__ BinWeights voxel_weights(float relx, float rely, cons
   return bin_weights(det_coord(relx, rely, k.c, k.s, pcent), k);
 }
 
+// acc + w * v per component, two components per instruction: the packed
+// FP32 multiply-add of compute capability 10.x rounds each component as
+// fmaf does, so results are those of four fmaf calls.
 __device__ __forceinline__ float4 f4_fma(float w, float4 v, float4 acc) {
-  acc.x = fmaf(w, v.x, acc.x);
-  acc.y = fmaf(w, v.y, acc.y);
-  acc.z = fmaf(w, v.z, acc.z);
-  acc.w = fmaf(w, v.w, acc.w);
-  return acc;
+  const float2 ww = make_float2(w, w);
+  const float2 lo = __ffma2_rn(ww, make_float2(v.x, v.y), make_float2(acc.x, acc.y));
+  const float2 hi = __ffma2_rn(ww, make_float2(v.z, v.w), make_float2(acc.z, acc.w));
+  return make_float4(lo.x, lo.y, hi.x, hi.y);
 }
 
 __device__ __forceinline__ float f4_fma(float w, float v, float acc) { return fmaf(w, v, acc); }

@@ -75,3 +75,23 @@ def test_reference_arm_as_two_ranks_prints_one_line():
     line = json.loads(lines[0])
     assert line["impl"] == "reference" and line["value"] > 0
     assert line["e2e"]["h2d_bytes_per_step"] == 0
+
+
+def test_metric_and_l2_note_follow_the_configuration():
+    """The headline configuration keeps the published metric's name; other
+    sizes name their own, and the L2 note says whether the inputs exceed L2
+    (the steps are not separated by an L2 flush)."""
+    import argparse
+
+    sys.path.insert(0, str(ROOT))
+    import bench
+
+    head = argparse.Namespace(size=512, angles=192)
+    assert bench.metric_name(head) == bench.METRIC
+    small = argparse.Namespace(size=128, angles=192)
+    assert "128³/192" in bench.metric_name(small)
+    assert bench.metric_name(small) != bench.METRIC
+    assert bench.l2_note(512**3 * 4, 192 * 512 * 512 * 4).startswith("inputs larger than L2")
+    assert "warm-L2" in bench.l2_note(128**3 * 4, 192 * 128 * 128 * 4)
+    # one input below L2 is enough for the warm-L2 label
+    assert "warm-L2" in bench.l2_note(512**3 * 4, 8 * 512 * 512 * 4)

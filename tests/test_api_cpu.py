@@ -16,6 +16,27 @@ def test_public_surface():
         assert callable(getattr(vp._CU, name))
 
 
+def test_signatures_match_reference():
+    """forward(x, angles, y, z_order=0, block_size=[8, 8, 8]) and
+    backward(y, angles, x, ...) as in wrappers.py:28,76: the output argument
+    is positional with no default."""
+    import inspect
+
+    for fn, names in ((vp.forward, ["x", "angles", "y"]), (vp.backward, ["y", "angles", "x"])):
+        params = list(inspect.signature(fn).parameters.values())
+        assert [p.name for p in params] == names + ["z_order", "block_size"]
+        assert all(p.default is inspect.Parameter.empty for p in params[:3])
+        assert params[3].default == 0
+        assert params[4].default == [8, 8, 8]
+    with pytest.raises(TypeError):
+        vp.forward(np.zeros((4, 4, 2), np.float32), np.zeros(3, np.float32))
+    # the extension's functions: (in, out, angles, block_size=[8, 8, 8]); the
+    # default is held as a tuple (block_size is accepted and ignored)
+    for name in ["forward_z0", "backward_z0", "forward_z2", "backward_z2"]:
+        params = list(inspect.signature(getattr(vp._CU, name)).parameters.values())
+        assert len(params) == 4 and list(params[3].default) == [8, 8, 8]
+
+
 @pytest.mark.parametrize("z", [1, 3, -1])
 def test_bad_z_order_raises_key_error(z):
     # the reference dispatches through a dict (wrappers.py:44-47)

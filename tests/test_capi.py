@@ -107,3 +107,30 @@ def test_batch_validation_without_gpu():
 def test_batch_problem_layout_matches_header():
     # int op, flags, variant, reserved; 3 pointers; n_angles; 2 x int64[3]
     assert ctypes.sizeof(_lib.BatchProblem) == 16 + 3 * 8 + 8 + 48
+
+
+@pytest.mark.parametrize("lang", ["c99", "c++17"])
+def test_header_is_plain_c(lang, tmp_path):
+    """The public header stands alone as strict C99 and as C++ (no CUDA or
+    torch headers needed), so a C, cgo or ctypes caller can use it as is."""
+    import shutil
+    import subprocess
+
+    cc = shutil.which("gcc" if lang == "c99" else "g++")
+    if cc is None:
+        pytest.skip("no host compiler")
+    src = tmp_path / "use_header.c"
+    # a typed pointer to an entry point also checks its signature
+    src.write_text('#include "voxelproj_gb300.h"\n'
+                   "int main(void) {\n"
+                   "  vp_batch_problem p; (void)p;\n"
+                   "  int (*f)(const float*, int64_t, int64_t, int64_t, float*, int64_t, int64_t,\n"
+                   "           int64_t, const float*, int64_t, int, void*) = vp_forward_z0;\n"
+                   "  (void)f;\n"
+                   "  return 0;\n"
+                   "}\n")
+    cmd = [cc, "-Wall", "-Wextra", "-Werror", "-pedantic", "-fsyntax-only",
+           "-I", str(ROOT / "include")]
+    cmd += ["-std=c99", str(src)] if lang == "c99" else ["-std=c++17", "-x", "c++", str(src)]
+    res = subprocess.run(cmd, capture_output=True, text=True, timeout=60)
+    assert res.returncode == 0, res.stderr

@@ -25,13 +25,17 @@ def test_uneven_cubes_custom_ranges():
     assert all(s in (32, 48) and n in (5, 6) for s, n in got)
 
 
-class _FakeCuda(torch.Tensor):
-    """A CPU tensor that reports itself as a CUDA tensor, so that the check
-    of the named argument is the one that fails."""
+def _fake_cuda(t):
+    """t as a CPU tensor that reports itself as a CUDA tensor, so that the
+    check of another argument is the one that fails (defined when used, so
+    that collecting this file needs nothing of torch's subclassing)."""
 
-    @property
-    def is_cuda(self):
-        return True
+    class FakeCuda(torch.Tensor):
+        @property
+        def is_cuda(self):
+            return True
+
+    return t.as_subclass(FakeCuda)
 
 
 @pytest.mark.parametrize("name", ["in", "out", "angles"])
@@ -39,14 +43,14 @@ def test_problem_rejects_host_tensors(name):
     """Batched problems live on the device: a CPU tensor is refused by name
     before any pointer is taken."""
     tensors = {"in": torch.zeros(4, 4, 4), "out": torch.zeros(3, 4, 4), "angles": torch.zeros(3)}
-    args = [t if k == name else t.as_subclass(_FakeCuda) for k, t in tensors.items()]
+    args = [t if k == name else _fake_cuda(t) for k, t in tensors.items()]
     with pytest.raises(RuntimeError, match=f"batch {name} must be"):
         _problem("forward", *args, 0)
 
 
 def test_problem_rejects_non_3d_arrays():
-    x = torch.zeros(4, 16).as_subclass(_FakeCuda)
-    y = torch.zeros(3, 4, 4).as_subclass(_FakeCuda)
-    a = torch.zeros(3).as_subclass(_FakeCuda)
+    x = _fake_cuda(torch.zeros(4, 16))
+    y = _fake_cuda(torch.zeros(3, 4, 4))
+    a = _fake_cuda(torch.zeros(3))
     with pytest.raises(RuntimeError, match="3-D"):
         _problem("forward", x, y, a, 0)

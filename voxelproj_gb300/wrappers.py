@@ -186,6 +186,9 @@ def _host_call(fn_name, inp, out, angles, default_shape, kind):
     return result
 
 
+# block_size keeps the reference's list default (wrappers.py:28,76) so that
+# the signatures match exactly; it is handed to the extension functions,
+# which ignore it, and never mutated.
 def forward(x, angles, y, z_order=0, block_size=[8, 8, 8]):
     """Forward projection: returns y + A x (see module docstring)."""
     kind, device = _kind(x)

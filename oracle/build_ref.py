@@ -11,7 +11,12 @@ Only ``tests/golden/make_golden.py`` uses the result, to record the
 reference's outputs as golden fixtures.  The voxelproj_gb300 package never
 loads it.
 
-    python oracle/build_ref.py [--src DIR]     (default DIR: /root/reference/voxelproj/csrc)
+    python oracle/build_ref.py --src DIR
+    VOXELPROJ_REF_SRC=DIR python oracle/build_ref.py
+
+DIR is the reference's ``voxelproj/csrc`` directory (``voxelproj.cpp``,
+``projectors.cu`` and ``include/``), given by ``--src`` or else by the
+environment variable ``VOXELPROJ_REF_SRC``.
 """
 
 from __future__ import annotations
@@ -22,14 +27,25 @@ from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
 OUT = HERE / "_ref"
-DEFAULT_SRC = Path("/root/reference/voxelproj/csrc")
+SRC_ENV = "VOXELPROJ_REF_SRC"
+
+
+def source_dir(src: Path | str | None = None) -> Path:
+    """The reference's csrc directory: `src`, else $VOXELPROJ_REF_SRC."""
+    if src:
+        return Path(src)
+    env = os.environ.get(SRC_ENV)
+    if not env:
+        raise FileNotFoundError(f"give the reference's voxelproj/csrc directory with --src or "
+                                f"${SRC_ENV}")
+    return Path(env)
 
 
 def build(src: Path | None = None, verbose: bool = False):
     """Builds (or reuses) the reference extension and returns the module."""
     from torch.utils import cpp_extension
 
-    src = Path(src) if src else DEFAULT_SRC
+    src = source_dir(src)
     files = [src / "voxelproj.cpp", src / "projectors.cu"]
     for f in files:
         if not f.exists():

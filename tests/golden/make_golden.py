@@ -3,8 +3,8 @@
 Runs the reference voxelproj CUDA kernels (``voxelproj._CU``, built from the
 reference's sources by ``oracle/build_ref.py``) on small seeded inputs and
 writes ``tests/golden/reference_outputs.npz``.  The fixtures pin the oracle
-(tests/test_oracle_golden.py) and the GB300 kernels (tests/test_golden_gpu.py)
-to the reference.
+and the GB300 kernels to the reference (``tests/test_golden.py``: the oracle
+on CPU, the kernels under the ``gpu`` mark).
 
     python oracle/build_ref.py --src <dir holding voxelproj.cpp, projectors.cu>
     python tests/golden/make_golden.py --src <same dir>

@@ -44,9 +44,12 @@ METRIC = "GVU/s (voxel×angle) for A and Aᵀ at 512³/192 ang"
 def metric_name(args) -> str:
     """The headline metric's name for the headline workload; other sizes and
     angle counts carry their own in the same form."""
-    if (args.size, args.angles) == (512, 192):
+    if (args.size, args.angles, heights(args)) == (512, 192, 512):
         return METRIC
-    return f"GVU/s (voxel×angle) for A and Aᵀ at {args.size}³/{args.angles} ang"
+    if heights(args) == args.size:
+        return f"GVU/s (voxel×angle) for A and Aᵀ at {args.size}³/{args.angles} ang"
+    return (f"GVU/s (voxel×angle) for A and Aᵀ at {args.size}²×{heights(args)}/{args.angles} "
+            f"ang")
 UNIT = "GVU/s"
 # The reference's published timing (its README.md:58-59, RTX 3060, z_order 0,
 # 512^3, 192 angles, units taken as ms):
@@ -67,6 +70,8 @@ def parse_args():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--size", type=int, default=512)
+    ap.add_argument("--height", type=int, default=0,
+                    help="volume heights (0: as --size, a cube)")
     ap.add_argument("--angles", type=int, default=192)
     ap.add_argument("--z-order", type=int, default=0, choices=[0, 2])
     ap.add_argument("--trig", choices=["reference", "precise"], default="reference")
@@ -106,15 +111,22 @@ def whole_job_gvu_s(world: int, steps: int, vu_step: float, total_ms: float) -> 
     return world * steps * vu_step / (total_ms / 1e3) / 1e9
 
 
-def shapes(S, n, z):
-    xs = (S, S, S)
-    ys = (n, S, S) if z == 0 else (S, n, S)
+def heights(args) -> int:
+    return getattr(args, "height", 0) or args.size
+
+
+def shapes(S, n, z, H=None):
+    """x and y shapes of an S x S volume of H heights (a cube by default)."""
+    H = S if H is None else H
+    xs = (S, S, H) if z == 0 else (H, S, S)
+    ys = (n, S, H) if z == 0 else (H, n, S)
     return xs, ys
 
 
-def algorithmic_bytes(S, n, PX):
-    vol = S * S * S * 4
-    sino = n * PX * S * 4
+def algorithmic_bytes(S, n, PX, H=None):
+    H = S if H is None else H
+    vol = S * S * H * 4
+    sino = n * PX * H * 4
     return {"A": vol + 2 * sino, "AT": sino + 2 * vol}
 
 
@@ -208,13 +220,14 @@ class ClockSampler:
 
 # --------------------------------------------------------------- CPU legs --
 
-def cpu_sample(S, n, z, target_s, x_np=None):
+def cpu_sample(S, n, z, target_s, x_np=None, H=None):
     """Times the FP32 OpenMP CPU evaluation of A then A^T on a prefix of the
     angles, sized to take about target_s seconds; returns (GVU/s, cores,
     description)."""
     from oracle import oracle
 
-    xs, ys = shapes(S, n, z)
+    H = S if H is None else H
+    xs, ys = shapes(S, n, z, H)
     rng = np.random.default_rng(0)
     x = x_np if x_np is not None else rng.standard_normal(xs, dtype=np.float32)
     ang = np.linspace(0, np.pi, n).astype(np.float32)
@@ -231,8 +244,9 @@ def cpu_sample(S, n, z, target_s, x_np=None):
     dt = run(k)
     k = int(max(1, min(n, k * target_s / max(dt, 1e-3))))
     dt = run(k)
-    vu = 2 * S**3 * k
-    desc = (f"A then Aᵀ on the full {S}³ volume for the first {k} of {n} angles, "
+    vu = 2 * S * S * H * k
+    vol = f"{S}³" if H == S else f"{S}²×{H}"
+    desc = (f"A then Aᵀ on the full {vol} volume for the first {k} of {n} angles, "
             f"FP32 CPU restatement (oracle/vp_oracle.c), OpenMP")
     return vu / dt / 1e9, oracle.max_threads(), desc, k
 
@@ -243,15 +257,15 @@ def run_reference_arm(args, world, rank):
         return
     from oracle import oracle
 
-    S, n, z = args.size, args.angles, args.z_order
-    xs, ys = shapes(S, n, z)
+    S, n, z, H = args.size, args.angles, args.z_order, heights(args)
+    xs, ys = shapes(S, n, z, H)
     rng = np.random.default_rng(0)
     x = rng.standard_normal(xs, dtype=np.float32)
     ang = np.linspace(0, np.pi, n).astype(np.float32)
     y = np.zeros(ys, np.float32)
     xb = np.zeros(xs, np.float32)
     # size one step to ~3 s of CPU work so steps + warmup end within minutes
-    _, _, _, k = cpu_sample(S, n, z, 3.0, x)
+    _, _, _, k = cpu_sample(S, n, z, 3.0, x, H)
 
     def step():
         oracle.forward_f32_(x, y, ang, z, 0, k)
@@ -263,9 +277,10 @@ def run_reference_arm(args, world, rank):
     for _ in range(args.steps):
         step()
     dt = time.perf_counter() - t0
-    vu = 2 * S**3 * k * args.steps
+    vu = 2 * S * S * H * k * args.steps
     val = vu / dt / 1e9
-    sample = (f"each step: A then Aᵀ on the full {S}³ volume for the first {k} of {n} angles "
+    vol = f"{S}³" if H == S else f"{S}²×{H}"
+    sample = (f"each step: A then Aᵀ on the full {vol} volume for the first {k} of {n} angles "
               f"(FP32 CPU restatement, oracle/vp_oracle.c, OpenMP; the reference package has "
               f"no CPU implementation)")
     line = {
@@ -295,13 +310,15 @@ def l2_note(x_bytes: int, y_bytes: int) -> str:
 
 
 def workload_config(args):
-    S, n = args.size, args.angles
+    S, n, H = args.size, args.angles, heights(args)
+    vol = f"{S}³" if H == S else f"{S}²×{H}"
     return {
-        "workload": (f"A then Aᵀ, z_order {args.z_order}, {S}³ float32 volume N(0,1), {n} angles "
-                     f"linspace(0,π), detector width {S}"),
-        "volume": [S, S, S], "n_angles": n, "detector_width": S, "z_order": args.z_order,
+        "workload": (f"A then Aᵀ, z_order {args.z_order}, {vol} float32 volume N(0,1), {n} "
+                     f"angles linspace(0,π), detector width {S}"),
+        "volume": [S, S, H] if args.z_order == 0 else [H, S, S], "n_angles": n,
+        "detector_width": S, "z_order": args.z_order,
         "trig": args.trig,
-        "l2": l2_note(S**3 * 4, n * S * S * 4),
+        "l2": l2_note(S * S * H * 4, n * S * H * 4),
         "parallelism": "replicas (one independent problem per GPU)",
         "kernel_variants": {"A": args.variant_fwd or "default", "AT": args.variant_bwd or "default"},
     }
@@ -321,9 +338,9 @@ def run_ours(args, world, rank, local):
     op_f, op_b = (0, 1) if args.z_order == 0 else (2, 3)
     _lib.LIB.vp_set_kernel_variant(op_f, args.variant_fwd)
     _lib.LIB.vp_set_kernel_variant(op_b, args.variant_bwd)
-    S, n, z = args.size, args.angles, args.z_order
+    S, n, z, H = args.size, args.angles, args.z_order, heights(args)
     PX = S
-    xs, ys = shapes(S, n, z)
+    xs, ys = shapes(S, n, z, H)
     fwd = vp._CU.forward_z0 if z == 0 else vp._CU.forward_z2
     bwd = vp._CU.backward_z0 if z == 0 else vp._CU.backward_z2
 
@@ -373,7 +390,7 @@ def run_ours(args, world, rank, local):
     t_fwd = [e[0].elapsed_time(e[1]) for e in evs]
     t_bwd = [e[1].elapsed_time(e[2]) for e in evs]
     total_ms = max_over_ranks(total_ms, world, dev)
-    vu_step = 2 * S**3 * n
+    vu_step = 2 * S * S * H * n
     value = whole_job_gvu_s(world, args.steps, vu_step, total_ms)
     fwd_ms = statistics.mean(t_fwd)
     bwd_ms = statistics.mean(t_bwd)
@@ -384,7 +401,7 @@ def run_ours(args, world, rank, local):
         hbm_peak = peaks.get("hbm_gbs")
         peak_note = "measured" if hbm_peak else "fallback"
         hbm_peak = hbm_peak or 6800.0
-        alg = algorithmic_bytes(S, n, PX)
+        alg = algorithmic_bytes(S, n, PX, H)
         kern = "A" if fwd_ms >= bwd_ms else "AT"
         kname = KERNELS[(kern, z)]
         dur_s = (fwd_ms if kern == "A" else bwd_ms) / 1e3
@@ -402,9 +419,9 @@ def run_ours(args, world, rank, local):
         sms = torch.cuda.get_device_properties(dev).multi_processor_count
         clk = peaks.get("sm_max_mhz", 2070.0)
         fp32_peak = sms * 128 * 2 * clk * 1e6 / 1e12
-        flops = 2.0 * nnz * S  # one multiply-add per nonzero weight per height
+        flops = 2.0 * nnz * H  # one multiply-add per nonzero weight per height
         # the reference publishes A and A^T times for 512^3 / 192 angles, z_order 0
-        published = (S, n, args.z_order) == (512, 192, 0)
+        published = (S, n, args.z_order, H) == (512, 192, 0, 512)
         result = {
             "metric": metric_name(args), "value": round(value, 3), "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup,
@@ -417,9 +434,9 @@ def run_ours(args, world, rank, local):
                                  "no published figure for this configuration",
             "dtype": "f32", "data": "synthetic", "config": workload_config(args),
             "parts": {
-                "A": {"ms": round(fwd_ms, 4), "gvu_s": round(S**3 * n / fwd_ms / 1e6, 2),
+                "A": {"ms": round(fwd_ms, 4), "gvu_s": round(S * S * H * n / fwd_ms / 1e6, 2),
                       "kernel": KERNELS[("A", z)]},
-                "AT": {"ms": round(bwd_ms, 4), "gvu_s": round(S**3 * n / bwd_ms / 1e6, 2),
+                "AT": {"ms": round(bwd_ms, 4), "gvu_s": round(S * S * H * n / bwd_ms / 1e6, 2),
                        "kernel": KERNELS[("AT", z)]},
             },
             "roofline": {"bound": "hbm", "kernel": kname, "achieved": round(achieved, 2),
@@ -445,7 +462,7 @@ def run_ours(args, world, rank, local):
     if rank == 0 and result is not None and not args.no_e2e:
         result["e2e"] = e2e_leg(args, vp, x, ang_np, dev)
     if rank == 0 and result is not None and world == 1 and not args.no_cpu_baseline:
-        val, cores, desc, _ = cpu_sample(S, n, z, args.cpu_seconds)
+        val, cores, desc, _ = cpu_sample(S, n, z, args.cpu_seconds, None, H)
         result["cpu_baseline"] = {"value": round(val, 4), "unit": UNIT, "cores": cores,
                                   "kind": "port", "sample": desc}
     if rank == 0 and result is not None:
@@ -459,8 +476,8 @@ def e2e_leg(args, vp, x_dev, ang_np, dev):
     """Same step through voxelproj_gb300.forward/backward with pinned CPU
     tensors: every step copies x, the output containers and the sinogram to
     the device and reads both results back."""
-    S, n, z = args.size, args.angles, args.z_order
-    xs, ys = shapes(S, n, z)
+    S, n, z, H = args.size, args.angles, args.z_order, heights(args)
+    xs, ys = shapes(S, n, z, H)
     x_h = x_dev.cpu().pin_memory()
     y_h = torch.zeros(ys).pin_memory()
     xb_h = torch.zeros(xs).pin_memory()
@@ -478,8 +495,8 @@ def e2e_leg(args, vp, x_dev, ang_np, dev):
         step()
     torch.cuda.synchronize(dev)
     dt = (time.perf_counter() - t0) / k
-    vol, sino, a = 4 * S**3, 4 * n * S * S, 4 * n
-    return {"value": round(2 * S**3 * n / dt / 1e9, 3), "unit": UNIT,
+    vol, sino, a = 4 * S * S * H, 4 * n * S * H, 4 * n
+    return {"value": round(2 * S * S * H * n / dt / 1e9, 3), "unit": UNIT,
             "ms_per_step": round(dt * 1e3, 3),
             "h2d_bytes_per_step": vol + sino + a + sino + vol + a,
             "d2h_bytes_per_step": sino + vol,

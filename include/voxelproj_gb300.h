@@ -91,6 +91,24 @@ VP_API uint64_t vp_launch_count(void);
  * fall back to direct loads.  Synchronises the device. */
 VP_API uint64_t vp_wait_timeouts(void);
 
+/* Limits of this library's bounded device waits, for tests of their error
+ * paths; no counterpart in the reference.  They apply process-wide to
+ * launches enqueued from now on.  No wait can hang: each gives up at its
+ * limit, records it, and the kernel goes on (vp_wait_timeouts,
+ * vp_batch_error).
+ *   copy_polls   polls of a bulk copy's completion barrier in the staged
+ *                adjoint (backward z0 variant 9) before its block falls back
+ *                to plain loads: VP_WAIT_DEFAULT for the default (2^22), 0 to
+ *                make every such wait give up at once.
+ *   stage_spins  ~256 ns sleeps a batch stage waits for the stage before it
+ *                (0: the default, 2^24, about 4 s).
+ *   stage_extra  completions a batch stage waits for beyond those its
+ *                previous stage gives: 0 in operation; any other value makes
+ *                every stage wait run out.
+ * Returns VP_OK. */
+#define VP_WAIT_DEFAULT 0xFFFFFFFFu
+VP_API int vp_set_wait_limits(uint32_t copy_polls, uint32_t stage_spins, uint32_t stage_extra);
+
 /* Kernel variant selection, used by the autotuner and for measurements.
  * op: 0 = forward z0, 1 = backward z0, 2 = forward z2, 3 = backward z2;
  * variant 0 = automatic (default).  Unknown variants fall back to automatic.

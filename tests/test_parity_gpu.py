@@ -186,7 +186,8 @@ def test_backward_variants_store_mode_via_z2(variant, H):
     assert rel_err(outs[0] - x0, oracle.backward(y, ang, SY, SX, 2)) <= tol.ref_vs_fp64(PX)
 
 
-@pytest.mark.parametrize("variant", [1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12, 13])
+@pytest.mark.parametrize("variant", [1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12, 13, 14, 15, 16, 17,
+                                     19])
 @pytest.mark.parametrize("geom", [(23, 37, 132, 61, 50, "wide"), (9, 6, 8, 40, 11, "axes"),
                                   (70, 64, 256, 96, 90, "rand"), (30, 21, 260, 33, 40, "rand"),
                                   (26, 31, 1024, 23, 36, "wide")],
@@ -214,7 +215,7 @@ def test_forward_variants(variant, geom):
     assert err <= tol.ref_vs_fp64(max(SY, SX, PX))
 
 
-@pytest.mark.parametrize("variant", [1, 5, 7, 8, 9, 12, 13])
+@pytest.mark.parametrize("variant", [1, 5, 7, 8, 9, 12, 13, 14, 16, 17, 19])
 @pytest.mark.parametrize("H", [36, 260, 512])
 def test_forward_variants_store_mode_via_z2(variant, H):
     """The forward's first slab launch writes the z_order 2 scratch in store
@@ -266,4 +267,38 @@ def test_adjoint_bulk_copy_variant_is_bit_identical(geom):
     finally:
         _lib.LIB.vp_set_kernel_variant(1, 0)
     assert torch.equal(outs[7], outs[9])
+    assert _lib.LIB.vp_wait_timeouts() == before
+
+
+@pytest.mark.parametrize("geom", [(64, 64, 256, 96, 64, "pi"), (70, 64, 260, 97, 90, "rand"),
+                                  (40, 48, 512, 70, 52, "wide"), (128, 96, 384, 200, 130, "pi"),
+                                  (33, 29, 132, 45, 40, "axes"), (96, 96, 256, 1024, 96, "pi"),
+                                  (200, 180, 256, 13, 150, "pi")],
+                         ids=lambda g: "x".join(map(str, g[:5])) + g[5])
+@pytest.mark.parametrize("variant,plain", [(17, 10), (19, 10)])
+def test_staged_forward_is_bit_identical(geom, variant, plain):
+    """The aligned forms (four aligned neighbouring angles per block; 17
+    stages the volume in shared memory by tensor copies, 19 loads it plainly)
+    sum the same candidates in the same order as variant 10 with the same 64
+    MB class slabs, so the results are equal bit for bit:
+    sorted and unsorted angles, angle counts not a multiple of the group,
+    partial height chunks, rectangular volumes, narrow and wide detectors."""
+    from voxelproj_gb300 import _lib
+
+    SY, SX, H, n, PX, kind = geom
+    ang = torch.tensor(angle_set(kind, n, 96), device="cuda")
+    x = torch.tensor(seeded((SY, SX, H), 37), device="cuda")
+    y0 = torch.tensor(seeded((n, PX, H), 38), device="cuda")
+    before = _lib.LIB.vp_wait_timeouts()
+    outs = {}
+    try:
+        for v in (plain, variant):
+            _lib.LIB.vp_set_kernel_variant(0, v)
+            yo = y0.clone()
+            vp._CU.forward_z0(x, yo, ang)
+            torch.cuda.synchronize()
+            outs[v] = yo
+    finally:
+        _lib.LIB.vp_set_kernel_variant(0, 0)
+    assert torch.equal(outs[plain], outs[variant])
     assert _lib.LIB.vp_wait_timeouts() == before

@@ -57,6 +57,7 @@ SIGNATURES = {
     "vp_last_cuda_error": (_I, []),
     "vp_launch_count": (ctypes.c_uint64, []),
     "vp_wait_timeouts": (ctypes.c_uint64, []),
+    "vp_set_wait_limits": (_I, [ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32]),
     "vp_set_kernel_variant": (_I, [_I, _I]),
     "vp_get_kernel_variant": (_I, [_I]),
     "vp_forward_z0": (_I, [_P, _I64, _I64, _I64, _P, _I64, _I64, _I64, _P, _I64, _I, _P]),

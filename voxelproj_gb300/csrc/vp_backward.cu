@@ -16,6 +16,8 @@
 #include <cuda_runtime.h>
 #include <cudaTypedefs.h>
 
+#include <atomic>
+
 #include "vp_bp_block.cuh"
 #include "vp_bp_runs.cuh"
 #include "vp_bp_runs_tma.cuh"
@@ -180,6 +182,38 @@ __global__ void __launch_bounds__(32 * BPR_WARPS, R == 8 ? 5 : 0)
 // Bounded-wait timeouts of this library's kernels (0 in correct operation).
 __device__ unsigned long long g_wait_timeouts = 0;
 
+// Polls of a copy's completion barrier before a block of the bulk-copy
+// adjoint falls back to plain loads (vp_set_wait_limits; tests lower it).
+std::atomic<unsigned> g_copy_polls{tma::kTmaMaxPolls};
+
+}  // namespace
+
+void set_copy_wait_polls(unsigned polls, bool use_default) {
+  g_copy_polls.store(use_default ? tma::kTmaMaxPolls : polls);
+}
+
+unsigned copy_wait_polls() { return g_copy_polls.load(); }
+
+cudaError_t wait_timeout_counter(unsigned long long** out) {
+  static std::atomic<unsigned long long*> addr[64] = {};
+  int dev = 0;
+  const cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+  unsigned long long* p = addr[dev].load(std::memory_order_acquire);
+  if (p == nullptr) {
+    void* sym = nullptr;
+    const cudaError_t e2 = cudaGetSymbolAddress(&sym, g_wait_timeouts);
+    if (e2 != cudaSuccess) return e2;
+    p = static_cast<unsigned long long*>(sym);
+    addr[dev].store(p, std::memory_order_release);
+  }
+  *out = p;
+  return cudaSuccess;
+}
+
+namespace {
+
 // The run adjoint with 8 heights per lane and each angle's bin window staged
 // once per block by bulk copies (vp_bp_runs_tma.cuh): 4 compute warps on a
 // 4 x 4 voxel tile (run_origin) and a copy warp.  Blocks that cannot stage (a
@@ -191,7 +225,7 @@ __global__ void __launch_bounds__(TMA_THREADS, 4)
     bp_z0_runs_tma_kernel(const float* __restrict__ y, float* __restrict__ x,
                           const float* __restrict__ angles, Geom g, int nrun_major,
                           int run_base, int run_end, int row_end, int accumulate,
-                          const __grid_constant__ CUtensorMap ymap) {
+                          unsigned copy_polls, const __grid_constant__ CUtensorMap ymap) {
   extern __shared__ __align__(128) unsigned char tma_smem[];
   TmaBlockSmem& sm = *reinterpret_cast<TmaBlockSmem*>(tma_smem);
   const int lane = threadIdx.x & 31;
@@ -212,7 +246,7 @@ __global__ void __launch_bounds__(TMA_THREADS, 4)
   run_origin<PASS>(run, nrun_major, &xi0, &yi0);
   if (staged) {
     bp_runs_tma_block<PASS>(y, x, angles, g, xi0, yi0, h0, accumulate, sm, &ymap,
-                            &g_wait_timeouts);
+                            &g_wait_timeouts, copy_polls);
     return;
   }
   if (w >= TMA_WARPS || run >= run_end || yi0 >= row_end) return;
@@ -328,26 +362,11 @@ cudaError_t launch_bp_z0_block(const float* y, float* x, const float* angles, co
 // The sinogram as a 3-D tensor (heights, bins, angles) with boxes of 256
 // heights x TMA_NBMAX bins x 1 angle, for the staged adjoint.
 cudaError_t sinogram_tensor_map(const float* y, const Geom& g, CUtensorMap* map) {
-  static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
-  if (encode == nullptr) {
-    void* fn = nullptr;
-    cudaDriverEntryPointQueryResult q;
-    const cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000,
-                                                           cudaEnableDefault, &q);
-    if (e != cudaSuccess) return e;
-    if (q != cudaDriverEntryPointSuccess || fn == nullptr) return cudaErrorNotSupported;
-    encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
-  }
-  const cuuint64_t dims[3] = {(cuuint64_t)g.Hy, (cuuint64_t)g.PX, (cuuint64_t)g.n_ang};
-  const cuuint64_t strides[2] = {(cuuint64_t)g.Hy * sizeof(float),
-                                 (cuuint64_t)g.PX * g.Hy * sizeof(float)};
-  const cuuint32_t box[3] = {(cuuint32_t)TMA_BIN_FLOATS, (cuuint32_t)TMA_NBMAX, 1};
-  const cuuint32_t estride[3] = {1, 1, 1};
-  const CUresult r = encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float*>(y), dims,
-                            strides, box, estride, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                            CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-  return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
+  const uint64_t dims[3] = {(uint64_t)g.Hy, (uint64_t)g.PX, (uint64_t)g.n_ang};
+  const uint64_t strides[2] = {(uint64_t)g.Hy * sizeof(float),
+                               (uint64_t)g.PX * g.Hy * sizeof(float)};
+  const uint32_t box[3] = {(uint32_t)TMA_BIN_FLOATS, (uint32_t)TMA_NBMAX, 1};
+  return tma::encode_3d_f32(map, y, dims, strides, box);
 }
 
 cudaError_t launch_bp_z0_runs_tma(const float* y, float* x, const float* angles, const Geom& g,
@@ -355,11 +374,13 @@ cudaError_t launch_bp_z0_runs_tma(const float* y, float* x, const float* angles,
   CUtensorMap ymap;
   cudaError_t e0m = sinogram_tensor_map(y, g, &ymap);
   if (e0m != cudaSuccess) return e0m;
-  static bool configured[64] = {};
+  // per device, once; two threads setting the same attributes at once is
+  // harmless, and the flag is atomic
+  static std::atomic<bool> configured[64] = {};
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
-  if (dev >= 0 && dev < 64 && !configured[dev]) {
+  if (dev < 0 || dev >= 64 || !configured[dev].load(std::memory_order_acquire)) {
     // the attribute is per device; setting it twice is harmless
     for (const void* k : {reinterpret_cast<const void*>(bp_z0_runs_tma_kernel<0>),
                           reinterpret_cast<const void*>(bp_z0_runs_tma_kernel<1>)}) {
@@ -369,7 +390,7 @@ cudaError_t launch_bp_z0_runs_tma(const float* y, float* x, const float* angles,
         e = cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
       if (e != cudaSuccess) return e;
     }
-    configured[dev] = true;
+    if (dev >= 0 && dev < 64) configured[dev].store(true, std::memory_order_release);
   }
   dim3 block(TMA_THREADS);
   const unsigned hchunks = ceil_div(g.H, 32 * 8);
@@ -380,7 +401,8 @@ cudaError_t launch_bp_z0_runs_tma(const float* y, float* x, const float* angles,
   if (e0 > b0) {
     bp_z0_runs_tma_kernel<0><<<dim3(ceil_div(e0 - b0, TMA_WARPS), hchunks), block,
                                kTmaBlockSmem, stream>>>(y, x, angles, g, nmaj0, (int)b0,
-                                                        (int)e0, row_hi, g.accumulate, ymap);
+                                                        (int)e0, row_hi, g.accumulate,
+                                                        g_copy_polls.load(), ymap);
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
   }
@@ -389,7 +411,8 @@ cudaError_t launch_bp_z0_runs_tma(const float* y, float* x, const float* angles,
   if (e1 > b1) {
     bp_z0_runs_tma_kernel<1><<<dim3(ceil_div(e1 - b1, TMA_WARPS), hchunks), block,
                                kTmaBlockSmem, stream>>>(y, x, angles, g, g.SX, (int)b1,
-                                                        (int)e1, row_hi, 1, ymap);
+                                                        (int)e1, row_hi, 1,
+                                                        g_copy_polls.load(), ymap);
     return cudaGetLastError();
   }
   return cudaSuccess;

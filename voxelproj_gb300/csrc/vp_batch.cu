@@ -30,12 +30,16 @@
 // s-1, on the stage's counter.  Items are taken in increasing order, so every
 // task a waiter depends on was taken earlier by a block that is already
 // running: the wait always ends.  It is bounded anyway: after ~4 s of spinning
-// it records an error (vp_batch_error) and writes regardless.
+// it records an error (vp_batch_error) and writes regardless.  The bound is a
+// kernel argument; vp_set_wait_limits lowers it, or makes every stage wait
+// need one completion more than its stage gives, so that tests can drive the
+// error path without any fault.
 //
 // A run allocates and synchronises nothing, so it can be captured in a CUDA
 // graph and replayed.
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cstdint>
 #include <cstring>
 #include <new>
@@ -58,6 +62,13 @@ constexpr int BATCH_WARPS = BATCH_THREADS / 32;
 static_assert(BATCH_WARPS == FP0_WARPS && BATCH_WARPS == BPB_WARPS &&
                   BATCH_WARPS == BPR_WARPS, "4 warps per block");
 constexpr unsigned kMaxSpins = 1u << 24;  // x ~256 ns sleeps: ~4 s
+
+// Stage-wait limits of a run: sleeps before giving up, and completions a
+// stage waits for beyond what its previous stage gives (0 in operation).
+struct WaitLimits {
+  unsigned spins;
+  unsigned extra;
+};
 
 enum BatchKind : int { K_FWD = 0, K_BWD_RUNS = 1, K_BWD_BLOCK = 2 };
 
@@ -98,12 +109,13 @@ struct StageWait {
   const unsigned* counter;
   unsigned target;
   int* error;
+  unsigned limit;  // sleeps before giving up
   static constexpr bool coherent = true;
   __device__ __forceinline__ void operator()() const {
     if ((threadIdx.x & 31) == 0) {
       unsigned spins = 0;
       while (*(volatile const unsigned*)counter < target) {
-        if (++spins > kMaxSpins) {
+        if (++spins > limit) {
           atomicExch(error, 1);
           break;
         }
@@ -120,14 +132,15 @@ struct StageWait {
 struct WaitSlot {
   unsigned* counter;
   int* error;
-  unsigned target;
+  unsigned target;  // 0: no wait (the first stage)
+  unsigned limit;
 };
 
 struct SlotWait {
   const WaitSlot* slot;
   static constexpr bool coherent = true;
   __device__ __forceinline__ void operator()() const {
-    if (slot->target > 0) StageWait{slot->counter, slot->target, slot->error}();
+    if (slot->target > 0) StageWait{slot->counter, slot->target, slot->error, slot->limit}();
   }
 };
 
@@ -146,14 +159,16 @@ __device__ __forceinline__ void signal_done(unsigned* counter) {
 template <int R, bool FULL>
 __device__ __forceinline__ void run_fwd_item(const BatchDesc& d, int stage, int in_stage,
                                              int hc, BatchSmem& sm, WaitSlot* slot, int w,
-                                             int lane, unsigned* counters, int* error) {
+                                             int lane, unsigned* counters, int* error,
+                                             const WaitLimits& lim) {
   constexpr int UN = R == 8 ? 2 : FP0_UNROLL;  // as the single-problem kernels
   const int a = in_stage / d.units;
   const int bg = in_stage - a * d.units;
   const Slab slab = slab_of(stage, d.cls, d.wy, d.wx, d.g.SY, d.g.SX);
   if (lane == 0)
     *slot = WaitSlot{counters + d.counter_base + ((size_t)hc * d.g.n_ang + a) * d.units + bg,
-                     error, (unsigned)(stage * BATCH_WARPS)};
+                     error, stage > 0 ? (unsigned)(stage * BATCH_WARPS) + lim.extra : 0u,
+                     lim.spins};
   __syncwarp();
   const int p0 = (bg * BATCH_WARPS + w) * 4;
   const int h = hc * 32 * R + lane * 4;
@@ -166,7 +181,8 @@ __device__ __forceinline__ void run_fwd_item(const BatchDesc& d, int stage, int 
 template <int R, bool FULL>
 __device__ __forceinline__ void run_bwd_runs_item(const BatchDesc& d, int stage, int grp,
                                                   int hc, BatchSmem& sm, int w, int lane,
-                                                  unsigned* counters, int* error) {
+                                                  unsigned* counters, int* error,
+                                                  const WaitLimits& lim) {
   unsigned* ctr = counters + d.counter_base + hc * d.nstages + stage;
   const int run = grp * BATCH_WARPS + w;
   const int h = hc * 32 * R + lane * 4;
@@ -177,7 +193,8 @@ __device__ __forceinline__ void run_bwd_runs_item(const BatchDesc& d, int stage,
       bp_runs_warp<0, R, NoWait, false, FULL>(d.in, d.out, d.angles, d.g, xi0, yi0, h, 1,
                                               sm.runs.tab[w], sm.runs.alist[w]);
   } else if (run < d.nruns1) {
-    const StageWait wt{ctr - 1, (unsigned)(d.groups0 * BATCH_WARPS), error};
+    const StageWait wt{ctr - 1, (unsigned)(d.groups0 * BATCH_WARPS) + lim.extra, error,
+                       lim.spins};
     bp_runs_warp<1, R, StageWait, false, FULL>(d.in, d.out, d.angles, d.g, run % d.g.SX,
                                                (run / d.g.SX) * RUN, h, 1, sm.runs.tab[w],
                                                sm.runs.alist[w], wt);
@@ -217,7 +234,7 @@ template <int BODY>
 __global__ void __launch_bounds__(BATCH_THREADS, batch_min_blocks(BODY))
     batch_kernel(const BatchDesc* __restrict__ descs, int ndesc, long long total,
                  unsigned long long* __restrict__ next, unsigned* __restrict__ counters,
-                 int* __restrict__ error) {
+                 int* __restrict__ error, WaitLimits lim) {
   __shared__ BatchSmem sm;
   __shared__ WaitSlot slots[BATCH_WARPS];
   __shared__ long long s_item;
@@ -246,13 +263,13 @@ __global__ void __launch_bounds__(BATCH_THREADS, batch_min_blocks(BODY))
       const int per_stage = d.g.n_ang * d.units;
       const int stage = in_chunk / per_stage;
       run_fwd_item<R, BODY == B_FWD8F>(d, stage, in_chunk - stage * per_stage, hc, sm,
-                                       &slots[w], w, lane, counters, error);
+                                       &slots[w], w, lane, counters, error, lim);
     } else if (BODY == B_BWD8 || BODY == B_BWD8F || d.kind == K_BWD_RUNS) {
       constexpr int R = (BODY == B_BWD8 || BODY == B_BWD8F) ? 8 : 4;
       const bool first = in_chunk < d.groups0;
       run_bwd_runs_item<R, BODY == B_BWD8F>(d, first ? 0 : 1,
                                             first ? in_chunk : in_chunk - d.groups0, hc, sm, w,
-                                            lane, counters, error);
+                                            lane, counters, error, lim);
     } else {
       const int bidx = in_chunk * BATCH_WARPS + w;
       if (bidx < d.nblocks)
@@ -267,7 +284,7 @@ __global__ void __launch_bounds__(BATCH_THREADS, batch_min_blocks(BODY))
 unsigned ceil_div_u(long long a, long long b) { return (unsigned)((a + b - 1) / b); }
 
 using BatchKernelFn = void (*)(const BatchDesc*, int, long long, unsigned long long*, unsigned*,
-                               int*);
+                               int*, WaitLimits);
 
 const void* batch_kernel_for(int body) {
   static const BatchKernelFn fns[NBODIES] = {batch_kernel<B_FWD4>, batch_kernel<B_FWD8>,
@@ -277,6 +294,16 @@ const void* batch_kernel_for(int body) {
 }
 
 }  // namespace
+
+// Stage-wait limits of the runs enqueued from now on (set_stage_wait_limits).
+std::atomic<unsigned> g_stage_spins{kMaxSpins};
+std::atomic<unsigned> g_stage_extra{0};
+
+void set_stage_wait_limits(unsigned spins, unsigned extra) {
+  g_stage_spins.store(spins ? spins : kMaxSpins);
+  g_stage_extra.store(extra);
+}
+
 }  // namespace vp
 
 struct vp_batch_plan {
@@ -306,9 +333,9 @@ int part_desc(const vp_batch_problem& p, const vp::Geom& g, const float* in, flo
   d->out = out;
   d->angles = p.angles;
   if (p.op == VP_OP_FORWARD) {
-    // the single-problem forward's plan for this variant (0: its default)
-    const vp::Fp0Plan pl = vp::forward_z0_plan(g, true, p.variant);
-    if (pl.KW != 4 || pl.agroup || pl.split ||
+    // the single-problem forward's plan for this variant (0: variant 10)
+    const vp::Fp0Plan pl = vp::forward_z0_plan(g, true, p.variant ? p.variant : 10);
+    if (pl.KW != 4 || pl.agroup || pl.split || pl.staged ||
         (pl.R == 8 ? pl.un != 2 : pl.un != vp::detail::FP0_UNROLL))
       return VP_ERR_BATCH;  // bodies the batch does not carry
     d->kind = vp::K_FWD;
@@ -388,7 +415,7 @@ int batch_desc(const vp_batch_problem& p, std::vector<vp::BatchDesc>* out) {
   // heights per lane of the first part
   int R = 4;
   if (fwd)
-    R = vp::forward_z0_plan(g, true, p.variant).R;
+    R = vp::forward_z0_plan(g, true, p.variant ? p.variant : 10).R;
   else if ((p.variant == 0 || p.variant == 7) && H > 128)
     R = 8;
   const int H8 = R == 8 ? vp::r8_heights(g.H) : g.H;
@@ -483,13 +510,14 @@ int vp_batch_run(vp_batch_plan* plan, void* stream) {
   cudaError_t e = cudaMemsetAsync(plan->d_next, 0, vp::NBODIES * sizeof(unsigned long long), st);
   if (e == cudaSuccess && plan->ncounters > 0)
     e = cudaMemsetAsync(plan->d_counters, 0, (size_t)plan->ncounters * sizeof(unsigned), st);
+  vp::WaitLimits lim{vp::g_stage_spins.load(), vp::g_stage_extra.load()};
   int launched = 0;
   for (int b = 0; b < vp::NBODIES && e == cudaSuccess; ++b) {
     if (plan->items[b] == 0) continue;
     const vp::BatchDesc* descs = plan->d_descs + plan->first[b];
     unsigned long long* next = plan->d_next + b;
     void* args[] = {&descs, &plan->ndesc[b], &plan->items[b], &next, &plan->d_counters,
-                    &plan->d_error};
+                    &plan->d_error, &lim};
     e = cudaLaunchKernel(vp::batch_kernel_for(b), dim3(plan->grid[b]), dim3(vp::BATCH_THREADS),
                          args, 0, st);
     ++launched;

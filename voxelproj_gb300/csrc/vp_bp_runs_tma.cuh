@@ -19,8 +19,10 @@
 //
 // Every wait is bounded (tma::mbar_wait).  When one runs out the block sets a
 // shared flag: no more copies are issued, every warp computes the rest from
-// global memory (results stay right), and before the block exits the copy
-// warp waits once more, bounded, for the stages with copies outstanding.
+// global memory (results stay right), waits still in progress give up, and
+// before the block exits the copy warp waits once more, bounded, for the
+// stages with copies outstanding.  A compute warp's wait for a stage's copy
+// polls at most copy_polls times (the kernel's argument).
 #pragma once
 
 #include "vp_bp_runs.cuh"
@@ -136,7 +138,8 @@ __device__ __forceinline__ void bp_runs_tma_block(const float* __restrict__ y,
                                                   const Geom& g, int xi0, int yi0, int h0,
                                                   int accumulate, TmaBlockSmem& sm,
                                                   const CUtensorMap* ymap,
-                                                  unsigned long long* timeouts) {
+                                                  unsigned long long* timeouts,
+                                                  unsigned copy_polls) {
   const int lane = threadIdx.x & 31;
   const int w = threadIdx.x >> 5;
   const bool copier = w == TMA_WARPS;
@@ -179,9 +182,9 @@ __device__ __forceinline__ void bp_runs_tma_block(const float* __restrict__ y,
           const int s = (slot + j) % TMA_STAGES;
           if (block_broken(sm)) break;
           if (used & (1u << s)) {  // wait until the compute warps released stage s
-            const bool ok = __all_sync(0xffffffffu,
-                                       tma::mbar_wait(&sm.empty[s], (empty_ph >> s) & 1u,
-                                                      timeouts));
+            const bool ok = __all_sync(
+                0xffffffffu, tma::mbar_wait(&sm.empty[s], (empty_ph >> s) & 1u, timeouts,
+                                            tma::kTmaMaxPolls, &sm.broken));
             if (!ok) {
               set_broken(sm);
               break;
@@ -203,7 +206,8 @@ __device__ __forceinline__ void bp_runs_tma_block(const float* __restrict__ y,
           bool staged = false;
           if (!block_broken(sm)) {
             staged = __all_sync(0xffffffffu,
-                                tma::mbar_wait(&sm.full[s], (full_ph >> s) & 1u, timeouts));
+                                tma::mbar_wait(&sm.full[s], (full_ph >> s) & 1u, timeouts,
+                                               copy_polls, &sm.broken));
             if (staged)
               full_ph ^= 1u << s;
             else

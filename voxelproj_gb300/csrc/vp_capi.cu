@@ -193,6 +193,12 @@ uint64_t vp_launch_count(void) { return g_launches.load(std::memory_order_relaxe
 
 uint64_t vp_wait_timeouts(void) { return vp::wait_timeouts(); }
 
+int vp_set_wait_limits(uint32_t copy_polls, uint32_t stage_spins, uint32_t stage_extra) {
+  vp::set_copy_wait_polls(copy_polls, copy_polls == VP_WAIT_DEFAULT);
+  vp::set_stage_wait_limits(stage_spins, stage_extra);
+  return VP_OK;
+}
+
 int vp_forward_z0(const float* x, int64_t x0, int64_t x1, int64_t x2, float* y, int64_t y0,
                   int64_t y1, int64_t y2, const float* angles, int64_t n_angles, int flags,
                   void* stream) {

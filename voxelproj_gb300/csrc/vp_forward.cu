@@ -15,9 +15,13 @@
 // sqrt(1/2)) only the indices whose xp lies within b + 1/2 (+ a small margin)
 // of the bins being gathered.  Voxels the margin admits needlessly get zero
 // weight from the closed form, so the margin only costs time.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
+#include <atomic>
+
 #include "vp_common.cuh"
+#include "vp_fp_staged.cuh"
 #include "vp_fp_z0.cuh"
 #include "vp_launch.h"
 
@@ -32,13 +36,16 @@ using namespace detail;
 // angle, or with AGROUP one bin run of neighbouring angles; blockIdx.z is the
 // height chunk of 32 * R heights.
 // The 8-height, 4-bin form is held to 7 resident blocks per SM (72
-// registers), its fastest occupancy.
+// registers), its fastest occupancy with 2 candidates in flight, and to 6
+// (80 registers, no spills) with 3 in flight.
 // With SPLIT a block takes 2 bin runs instead of 4, each by 2 warps that
 // gather half of the slab's major lines each: twice the blocks, each half as
 // long, so the last wave of a launch leaves less of the GPU idle.  The first
 // half writes (in the caller's mode); after a block barrier the second adds.
 template <int R, int KW, bool AGROUP, int UN, bool SPLIT = false, bool FULL = false>
-__global__ void __launch_bounds__(32 * FP0_WARPS, SPLIT ? (R == 8 ? 7 : 8) : (R == 8 && KW == 4 ? 7 : 0))
+__global__ void __launch_bounds__(32 * FP0_WARPS,
+                                  SPLIT ? (R == 8 ? 7 : 8)
+                                        : (R == 8 && KW == 4 ? (UN == 3 ? 6 : 7) : 0))
     fp_z0_kernel(const float* __restrict__ x, float* __restrict__ y,
                  const float* __restrict__ angles, Geom g, int a_base, Slab slab,
                  int accumulate) {
@@ -63,6 +70,67 @@ __global__ void __launch_bounds__(32 * FP0_WARPS, SPLIT ? (R == 8 ? 7 : 8) : (R 
     const int a = a_base + (AGROUP ? blockIdx.y * FP0_WARPS + w : blockIdx.y);
     fp_z0_warp<R, KW, UN, NoWait, FULL>(x, y, angles, g, p0, a, h, slab, accumulate, cand[w]);
   }
+}
+
+// The staged forward (vp_fp_staged.cuh): blocks of 4 compute warps on
+// neighbouring angles (blockIdx.y = angle group) and a copy warp; blockIdx.x
+// is the block's place on the group's aligned detector axis, offset by E
+// blocks; blockIdx.z the 256-height chunk.  NBOX voxels per staged line,
+// STAGES lines in flight; as many blocks per SM as shared memory holds (at
+// most 4).
+constexpr int fps_blocks_per_sm(size_t smem) {
+  return (int)((227u * 1024u) / (smem + 1024u)) < 4 ? (int)((227u * 1024u) / (smem + 1024u)) : 4;
+}
+
+template <bool FULL, int NBOX, int STAGES>
+__global__ void __launch_bounds__(FPS_THREADS,
+                                  fps_blocks_per_sm(sizeof(FpsSmem<NBOX, STAGES>)))
+    fp_z0_staged_kernel(const float* __restrict__ x, float* __restrict__ y,
+                        const float* __restrict__ angles, Geom g, int a_base, Slab slab,
+                        int accumulate, int E, unsigned long long* timeouts,
+                        unsigned copy_polls, const __grid_constant__ CUtensorMap map_rows,
+                        const __grid_constant__ CUtensorMap map_cols) {
+  extern __shared__ __align__(1024) unsigned char fps_raw[];
+  auto& sm = *reinterpret_cast<FpsSmem<NBOX, STAGES>*>(fps_raw);
+  const int lane = threadIdx.x & 31;
+  const int w = threadIdx.x >> 5;
+  const int a0 = a_base + (int)blockIdx.y * FPS_WARPS;
+  const int h0 = (int)blockIdx.z * 256;
+  const int bx = (int)blockIdx.x - E;
+  const FpsGroup G = fps_group(angles, g, slab, a0);  // alike in every thread
+  if (!G.aligned) {  // block-uniform: plain runs of 4 bins, as variant 10
+    if (w >= FPS_WARPS || !G.valid[w] || bx < 0 || 4 * bx >= g.PX) return;
+    fp_z0_warp<8, 4, 2, NoWait, FULL>(x, y, angles, g, 4 * bx, a0 + w, h0 + 4 * lane, slab,
+                                      accumulate, sm.cand[w]);
+    return;
+  }
+  fps_aligned_block<FULL, NBOX, STAGES>(x, y, angles, g, slab, accumulate, a0, h0, bx, -E,
+                                        (int)gridDim.x - 1 - E, G, sm, &map_rows, &map_cols,
+                                        timeouts, copy_polls);
+}
+
+// The aligned partition with plain loads (variant 19): 4 warps per block, no
+// copy warp, 7 blocks per SM as variant 10.
+template <bool FULL>
+__global__ void __launch_bounds__(32 * FPS_WARPS, 7)
+    fp_z0_aligned_kernel(const float* __restrict__ x, float* __restrict__ y,
+                         const float* __restrict__ angles, Geom g, int a_base, Slab slab,
+                         int accumulate, int E) {
+  __shared__ float4 cand[FPS_WARPS][Fp0Cap<4>::list];
+  const int lane = threadIdx.x & 31;
+  const int w = threadIdx.x >> 5;
+  const int a0 = a_base + (int)blockIdx.y * FPS_WARPS;
+  const int h0 = (int)blockIdx.z * 256;
+  const int bx = (int)blockIdx.x - E;
+  const FpsGroup G = fps_group(angles, g, slab, a0);
+  if (!G.aligned) {
+    if (!G.valid[w] || bx < 0 || 4 * bx >= g.PX) return;
+    fp_z0_warp<8, 4, 2, NoWait, FULL>(x, y, angles, g, 4 * bx, a0 + w, h0 + 4 * lane, slab,
+                                      accumulate, cand[w]);
+    return;
+  }
+  fps_plain_block<FULL>(x, y, angles, g, slab, accumulate, a0, h0, bx, -E,
+                        (int)gridDim.x - 1 - E, G, cand[w]);
 }
 
 // ---------------------------------------------------------------------------
@@ -145,6 +213,8 @@ struct Fp0Config {
   int slab_mb;    // volume bytes of one height chunk per slab launch
   bool cls;       // class slabs (rows for one angle class, columns for the other)
   bool split;     // two warps per bin run, each on half of the major lines
+  int staged;     // aligned neighbouring-angle forms (vp_fp_staged.cuh), 8 heights per
+                  // lane only: 1 = staged by tensor copies, 2 = plain loads; 0 = none
 };
 
 // Variants: 1 = 4 bins per warp, 4 heights per lane, warps of a block on
@@ -156,11 +226,15 @@ struct Fp0Config {
 // faster at 512^3 with 192 angles but misses L2 on the volume, 5.3 against
 // 4.6 GB of DRAM traffic per call); 12 = as 1
 // with class slabs of 32 MB; 13 = as 10 with two warps per bin run, each on
-// half of the slab's major lines (SPLIT).  Heights not in float4 run the scalar form of
+// half of the slab's major lines (SPLIT); 14 / 15 = as 10 / 11 with 3
+// candidates in flight at 6 blocks per SM; 16 = as 10 with the warps of a
+// block on neighbouring angles; 17 = as 10, four aligned neighbouring angles
+// per block, the volume staged through shared memory by tensor copies
+// (vp_fp_staged.cuh); 19 = the aligned angle groups with plain loads.  Heights not in float4 run the scalar form of
 // the same bin layout; 8-height variants on problems of at most 128 heights
 // run the 4-height form.
 Fp0Config fp0_config(const Geom& g, bool vec4, int variant) {
-  Fp0Config c{vec4 ? 4 : 1, 4, false, FP0_UNROLL, 32, false, false};
+  Fp0Config c{vec4 ? 4 : 1, 4, false, FP0_UNROLL, 32, false, false, 0};
   if (variant == 0) variant = 10;  // the default
   switch (variant) {
     case 2: c.KW = 8; break;
@@ -175,11 +249,17 @@ Fp0Config fp0_config(const Geom& g, bool vec4, int variant) {
     case 11: c.R = 8; c.un = 2; c.cls = true; c.slab_mb = 128; break;
     case 12: c.cls = true; break;
     case 13: c.R = 8; c.un = 2; c.cls = true; c.slab_mb = 64; c.split = true; break;
+    case 14: c.R = 8; c.un = 3; c.cls = true; c.slab_mb = 64; break;
+    case 15: c.R = 8; c.un = 3; c.cls = true; c.slab_mb = 128; break;
+    case 16: c.R = 8; c.un = 2; c.cls = true; c.slab_mb = 64; c.agroup = true; break;
+    case 17: c.R = 8; c.un = 2; c.cls = true; c.slab_mb = 64; c.staged = 1; break;
+    case 19: c.R = 8; c.un = 2; c.cls = true; c.slab_mb = 64; c.staged = 2; break;
     default: break;
   }
   if (c.R == 8 && (!vec4 || g.H <= 128)) {
     c.R = vec4 ? 4 : 1;
     c.un = FP0_UNROLL;
+    c.staged = 0;
   }
   return c;
 }
@@ -283,14 +363,111 @@ cudaError_t launch_slab_r(const Fp0Config& c, const SlabLaunch& L, cudaStream_t 
   return launch_slab<R, 4, false, FP0_UNROLL>(L, s, n);
 }
 
+// The volume as a 3-D tensor (heights, columns, rows) with boxes of one
+// staged line window: nbox voxels of a row (rows) or of a column (cols) x 256
+// heights.
+cudaError_t volume_tensor_maps(const float* x, const Geom& g, int nbox, CUtensorMap* rows,
+                               CUtensorMap* cols) {
+  const uint64_t dims[3] = {(uint64_t)g.Hx, (uint64_t)g.SX, (uint64_t)g.SY};
+  const uint64_t strides[2] = {(uint64_t)g.Hx * sizeof(float),
+                               (uint64_t)g.SX * g.Hx * sizeof(float)};
+  const uint32_t box_rows[3] = {(uint32_t)FPS_LINE, (uint32_t)nbox, 1};
+  const uint32_t box_cols[3] = {(uint32_t)FPS_LINE, 1, (uint32_t)nbox};
+  cudaError_t e = tma::encode_3d_f32(rows, x, dims, strides, box_rows);
+  if (e == cudaSuccess) e = tma::encode_3d_f32(cols, x, dims, strides, box_cols);
+  return e;
+}
+
+// Grid of the aligned forms: the detector in blocks of FPS_W lead bins, with
+// E blocks more on each side; angle groups; 256-height chunks.
+struct AlignedGrid {
+  int E;
+  unsigned gx;
+};
+AlignedGrid aligned_grid(const Geom& g) {
+  const int E = fps_margin(g.PX);
+  return AlignedGrid{E, (unsigned)((float)g.PX / FPS_W) + 1 + 2 * (unsigned)E};
+}
+
+template <bool FULL, int NBOX, int STAGES>
+cudaError_t launch_slab_staged(const SlabLaunch& L, cudaStream_t stream, int* launches) {
+  using Smem = FpsSmem<NBOX, STAGES>;
+  // per device, once: room for the kernel's dynamic shared memory
+  static std::atomic<bool> configured[64] = {};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= 64 || !configured[dev].load(std::memory_order_acquire)) {
+    e = cudaFuncSetAttribute(reinterpret_cast<const void*>(fp_z0_staged_kernel<FULL, NBOX, STAGES>),
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(Smem));
+    if (e != cudaSuccess) return e;
+    if (dev >= 0 && dev < 64) configured[dev].store(true, std::memory_order_release);
+  }
+  CUtensorMap rows, cols;
+  e = volume_tensor_maps(L.x, L.g, NBOX, &rows, &cols);
+  if (e != cudaSuccess) return e;
+  unsigned long long* timeouts = nullptr;
+  e = wait_timeout_counter(&timeouts);
+  if (e != cudaSuccess) return e;
+  const unsigned polls = copy_wait_polls();
+  Geom g = L.g;
+  g.n_ang = L.a_hi;
+  const AlignedGrid ag = aligned_grid(g);
+  const long long per_launch = (long long)kMaxGridYZ * FPS_WARPS;
+  for (long long a_base = L.a_lo; a_base < L.a_hi; a_base += per_launch) {
+    const long long na = L.a_hi - a_base < per_launch ? L.a_hi - a_base : per_launch;
+    dim3 grid(ag.gx, ceil_div(na, FPS_WARPS), ceil_div(g.H, 256));
+    fp_z0_staged_kernel<FULL, NBOX, STAGES><<<grid, FPS_THREADS, sizeof(Smem), stream>>>(
+        L.x, L.y, L.angles, g, (int)a_base, L.slab, L.accumulate, ag.E, timeouts, polls, rows,
+        cols);
+    if (launches) ++*launches;
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+template <bool FULL>
+cudaError_t launch_slab_aligned(const SlabLaunch& L, cudaStream_t stream, int* launches) {
+  Geom g = L.g;
+  g.n_ang = L.a_hi;
+  const AlignedGrid ag = aligned_grid(g);
+  const long long per_launch = (long long)kMaxGridYZ * FPS_WARPS;
+  for (long long a_base = L.a_lo; a_base < L.a_hi; a_base += per_launch) {
+    const long long na = L.a_hi - a_base < per_launch ? L.a_hi - a_base : per_launch;
+    dim3 grid(ag.gx, ceil_div(na, FPS_WARPS), ceil_div(g.H, 256));
+    fp_z0_aligned_kernel<FULL><<<grid, 32 * FPS_WARPS, 0, stream>>>(
+        L.x, L.y, L.angles, g, (int)a_base, L.slab, L.accumulate, ag.E);
+    if (launches) ++*launches;
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
 cudaError_t launch_slab_config(const Fp0Config& c, const SlabLaunch& L, cudaStream_t s, int* n) {
+  if (c.R == 8 && c.staged) {
+    const bool full = L.g.H % 256 == 0;
+    if (c.staged == 2)
+      return full ? launch_slab_aligned<true>(L, s, n) : launch_slab_aligned<false>(L, s, n);
+    return full ? launch_slab_staged<true, 12, 3>(L, s, n)
+                : launch_slab_staged<false, 12, 3>(L, s, n);
+  }
   if (c.R == 8) {
     if (c.KW == 8) return launch_slab<8, 8, false, 2>(L, s, n);
+    if (c.un == 2 && c.agroup) {
+      if (L.g.H % (32 * 8) == 0) return launch_slab<8, 4, true, 2, false, true>(L, s, n);
+      return launch_slab<8, 4, true, 2>(L, s, n);
+    }
     if (c.un == 2) {
       if (c.split) return launch_slab<8, 4, false, 2, true>(L, s, n);
       // whole chunks of 256 heights: the second float4 at a constant offset
       if (L.g.H % (32 * 8) == 0) return launch_slab<8, 4, false, 2, false, true>(L, s, n);
       return launch_slab<8, 4, false, 2>(L, s, n);
+    }
+    if (c.un == 3) {
+      if (L.g.H % (32 * 8) == 0) return launch_slab<8, 4, false, 3, false, true>(L, s, n);
+      return launch_slab<8, 4, false, 3>(L, s, n);
     }
     return launch_slab<8, 4, false, 4>(L, s, n);
   }
@@ -358,6 +535,7 @@ Fp0Plan forward_z0_plan(const Geom& g, bool vec4, int variant) {
   p.KW = c.KW;
   p.un = c.un;
   p.agroup = c.agroup;
+  p.staged = c.staged != 0;
   p.cls = c.cls;
   p.split = c.split;
   p.nslabs = fp0_slabs(g, c);
@@ -372,7 +550,8 @@ int launches_forward_z0(const float* x, const float* y, const Geom& g) {
   int n = 0;
   for (int i = 0; i < hp.n; ++i) {
     const Fp0Config c = fp0_config(hp.g[i], vec4, v);
-    const long long per = c.agroup ? (long long)kMaxGridYZ * FP0_WARPS : kMaxGridYZ;
+    const long long per =
+        (c.agroup || c.staged) ? (long long)kMaxGridYZ * FP0_WARPS : kMaxGridYZ;
     n += (int)(fp0_slabs(hp.g[i], c) * ceil_div(hp.g[i].n_ang, per));
   }
   return n;

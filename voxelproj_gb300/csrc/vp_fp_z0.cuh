@@ -57,10 +57,21 @@ constexpr int FP0_WARPS = 4;
 constexpr int FP0_QBITS = 4;   // q in [0, KW + 1]
 constexpr int FP0_UNROLL = 4;  // candidates whose loads are in flight together (R <= 4)
 
-// >= max candidates per major line: floor((KW + 2b + margin) / sqrt(1/2)) + 1
+// Most candidates one major line can hold: the window [t_lo, t_hi] is
+// KW + 2b + 2 * kWindowMargin bins wide with b <= sqrt(1/2), and neighbouring
+// voxels on the minor axis are at least sqrt(1/2) bins apart, so a line holds
+// at most floor((KW + sqrt(2) + 2 * margin) * sqrt(2)) + 1 of them (1.4142136
+// rounds sqrt(2) up).  The list builder clamps a line's count to the cap; the
+// assert below makes the clamp unreachable for every geometry, so no
+// candidate can be dropped.
+__host__ __device__ constexpr int fp0_line_bound(int KW) {
+  return (int)(((float)KW + 1.4142136f + 2.0f * kWindowMargin) * 1.4142136f) + 1;
+}
+
 template <int KW>
 struct Fp0Cap {
-  static constexpr int value = KW == 4 ? 10 : 15;
+  static constexpr int value = KW == 4 ? 8 : 14;
+  static_assert(value >= fp0_line_bound(KW), "a line's candidates must fit the list");
   // a warp's list: 32 lines of candidates, then padding for the loads of the
   // last group of FP0_UNROLL
   static constexpr int list = 32 * value + 4;
@@ -123,7 +134,7 @@ __host__ __device__ inline Slab slab_of(int k, bool cls, int wy, int wx, int SY,
   return Slab{y_lo, y_hi, x_lo, x_hi, 0, SY};
 }
 
-// One warp: angle a, bins [p0, p0 + KW), this lane's heights from h (LaneH:
+// One warp: angle a, bins [p0, p0 + nb) (nb <= KW), this lane's heights from h (LaneH:
 // R = 8 is [h, h + 4) and [h + 128, h + 132)), the voxels of slab s.  FULL:
 // every lane's heights are inside [0, H).
 // UN candidates are loaded together.  cand is this warp's shared candidate list of
@@ -135,7 +146,7 @@ __device__ __forceinline__ void fp_z0_warp(const float* __restrict__ x, float* _
                                            const float* __restrict__ angles, const Geom& g,
                                            int p0, int a, int h, const Slab& s,
                                            int accumulate, float4* cand,
-                                           const Wait& wait = Wait()) {
+                                           const Wait& wait = Wait(), int nb = KW) {
   using V = typename Vec<R>::T;
   constexpr int CAP = Fp0Cap<KW>::value;
   const int lane = threadIdx.x & 31;
@@ -161,7 +172,7 @@ __device__ __forceinline__ void fp_z0_warp(const float* __restrict__ x, float* _
   const float sh_major = minor_x ? k.s : k.c;
   const float inv_sh_minor = 1.0f / (minor_x ? k.c : k.s);
   const float t_lo = (float)p0 - 0.5f - k.b - kWindowMargin;
-  const float t_hi = (float)(p0 + KW) - 0.5f + k.b + kWindowMargin;
+  const float t_hi = (float)(p0 + nb) - 0.5f + k.b + kWindowMargin;
 
   V acc[KW];
 #pragma unroll
@@ -227,7 +238,7 @@ __device__ __forceinline__ void fp_z0_warp(const float* __restrict__ x, float* _
 #pragma unroll
   for (int b = 0; b < KW; ++b) {
     const int p = p0 + b;
-    if (p < g.PX)
+    if (p < g.PX && b < nb)
       store_lane<R, Wait::coherent>(y + ((size_t)a * g.PX + p) * g.Hy, lh, acc[b], accumulate);
   }
 }

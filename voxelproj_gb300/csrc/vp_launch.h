@@ -79,7 +79,7 @@ inline int r8_heights(int H) {
 // follows the same plan, so its results equal the single-problem kernel's.
 struct Fp0Plan {
   int R, KW, un;
-  bool agroup, cls, split;
+  bool agroup, cls, split, staged;
   int nslabs, wy, wx;
 };
 Fp0Plan forward_z0_plan(const Geom& g, bool vec4, int variant);
@@ -106,6 +106,16 @@ cudaError_t launch_forward_z0_rest(const float* x, float* y, const float* angles
 int backward_z0_row_step(const float* y, const float* x, const Geom& g);
 // Bounded waits in this library's kernels that ran out (synchronising read).
 unsigned long long wait_timeouts();
+// Limits of the bounded waits for launches enqueued from now on
+// (vp_set_wait_limits): polls of a bulk copy's barrier in the staged adjoint
+// (the default with use_default), and a batch stage's sleeps (0: default) and
+// extra completions waited for (0 in operation).
+void set_copy_wait_polls(unsigned polls, bool use_default);
+void set_stage_wait_limits(unsigned spins, unsigned extra);
+// The current limit of copy waits, and the device address (current device)
+// of the counter vp_wait_timeouts reads, for kernels of other units.
+unsigned copy_wait_polls();
+cudaError_t wait_timeout_counter(unsigned long long** out);
 cudaError_t launch_backward_z0_rows(const float* y, float* x, const float* angles,
                                     const Geom& g, int row_lo, int row_hi,
                                     cudaStream_t stream);

@@ -13,10 +13,46 @@
 
 #include <cuda.h>
 #include <cuda_runtime.h>
+#include <cudaTypedefs.h>
 #include <stdint.h>
 
 namespace vp {
 namespace tma {
+
+// cuTensorMapEncodeTiled, looked up once per process through the runtime (a
+// thread-safe static initialiser; no link against the driver library), or
+// nullptr where the driver does not offer it.
+inline PFN_cuTensorMapEncodeTiled_v12000 encode_tiled_fn() {
+  static const PFN_cuTensorMapEncodeTiled_v12000 fn = []() {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    const cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000,
+                                                           cudaEnableDefault, &q);
+    return (e == cudaSuccess && q == cudaDriverEntryPointSuccess)
+               ? reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(f)
+               : nullptr;
+  }();
+  return fn;
+}
+
+// A float32 3-D tensor map (dims and box innermost first; strides in bytes of
+// dims 1 and 2), zero fill outside the tensor.  The caller keeps the rules of
+// tiled copies: base 16-byte aligned, strides multiples of 16 bytes, box
+// inner extent a multiple of 16 bytes.
+inline cudaError_t encode_3d_f32(CUtensorMap* map, const float* base, const uint64_t dims[3],
+                                 const uint64_t strides[2], const uint32_t box[3]) {
+  const PFN_cuTensorMapEncodeTiled_v12000 encode = encode_tiled_fn();
+  if (encode == nullptr) return cudaErrorNotSupported;
+  const cuuint64_t d[3] = {dims[0], dims[1], dims[2]};
+  const cuuint64_t st[2] = {strides[0], strides[1]};
+  const cuuint32_t bx[3] = {box[0], box[1], box[2]};
+  const cuuint32_t estride[3] = {1, 1, 1};
+  const CUresult r = encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float*>(base),
+                            d, st, bx, estride, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                            CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
+}
 
 constexpr unsigned kTmaMaxPolls = 1u << 22;  // try_wait returns after a bounded time each
 
@@ -62,12 +98,18 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
   return done != 0;
 }
 
-// Waits until the barrier's phase of the given parity has completed; false
-// (and one count in *timeouts, from lane 0) if the bound ran out.
+// Waits until the barrier's phase of the given parity has completed, polling
+// at most `polls` times; false (and one count in *timeouts, from lane 0) if
+// the bound ran out.  With `abort`, the wait also gives up, uncounted, once
+// *abort is nonzero (another warp of the block gave up first).
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity,
-                                          unsigned long long* timeouts) {
-  for (unsigned i = 0; i < kTmaMaxPolls; ++i)
+                                          unsigned long long* timeouts,
+                                          unsigned polls = kTmaMaxPolls,
+                                          const volatile int* abort = nullptr) {
+  for (unsigned i = 0; i < polls; ++i) {
     if (mbar_try_wait(bar, parity)) return true;
+    if (abort && (i & 63u) == 63u && *abort) return false;
+  }
   if ((threadIdx.x & 31) == 0) atomicAdd(timeouts, 1ull);
   return false;
 }

@@ -92,12 +92,19 @@ struct BatchDesc {
   int nbx, nblocks, bgroups;
 };
 
-union BatchSmem {
+// Shared memory of each body: the forward bodies hold only their candidate
+// lists (as the single-problem forward, leaving the rest of the SM's unified
+// storage to L1); the adjoint bodies their run tables, or the 2x2 block
+// tables where the 4-height adjoint carries that variant too.
+struct FwdSmem {
   float4 cand[BATCH_WARPS][Fp0Cap<4>::list];
-  struct {
-    RunEntry tab[BATCH_WARPS][BPR_CHUNK];
-    int alist[BATCH_WARPS][BPR_LIST];
-  } runs;
+};
+struct RunsSmem {
+  RunEntry tab[BATCH_WARPS][BPR_CHUNK];
+  int alist[BATCH_WARPS][BPR_LIST];
+};
+union Bwd4Smem {
+  RunsSmem runs;
   struct {
     float4 tw[BATCH_WARPS][BPB_CHUNK][4];
     int2 tb[BATCH_WARPS][BPB_CHUNK];
@@ -156,9 +163,12 @@ __device__ __forceinline__ void signal_done(unsigned* counter) {
 // group) tile, written by one item per stage; its counter counts the warps
 // done on the tile, so a stage waits for the tile's previous stage alone.
 // FULL: the part's heights are whole 256-height chunks (R = 8).
+// Out of line: its own register allocation, apart from the persistent loop's
+// state (on the 64-cube workload the batched forward took 169.8 against
+// 179.2 ms inlined).
 template <int R, bool FULL>
-__device__ __forceinline__ void run_fwd_item(const BatchDesc& d, int stage, int in_stage,
-                                             int hc, BatchSmem& sm, WaitSlot* slot, int w,
+__device__ __noinline__ void run_fwd_item(const BatchDesc& d, int stage, int in_stage,
+                                             int hc, FwdSmem& sm, WaitSlot* slot, int w,
                                              int lane, unsigned* counters, int* error,
                                              const WaitLimits& lim) {
   constexpr int UN = R == 8 ? 2 : FP0_UNROLL;  // as the single-problem kernels
@@ -180,7 +190,7 @@ __device__ __forceinline__ void run_fwd_item(const BatchDesc& d, int stage, int 
 // FULL: the part's heights are whole 256-height chunks (R = 8).
 template <int R, bool FULL>
 __device__ __forceinline__ void run_bwd_runs_item(const BatchDesc& d, int stage, int grp,
-                                                  int hc, BatchSmem& sm, int w, int lane,
+                                                  int hc, RunsSmem& sm, int w, int lane,
                                                   unsigned* counters, int* error,
                                                   const WaitLimits& lim) {
   unsigned* ctr = counters + d.counter_base + hc * d.nstages + stage;
@@ -191,13 +201,13 @@ __device__ __forceinline__ void run_bwd_runs_item(const BatchDesc& d, int stage,
     run_origin<0>(run, (d.g.SX + RUN - 1) / RUN, &xi0, &yi0);
     if (run < d.nruns0 && yi0 < d.g.SY)
       bp_runs_warp<0, R, NoWait, false, FULL>(d.in, d.out, d.angles, d.g, xi0, yi0, h, 1,
-                                              sm.runs.tab[w], sm.runs.alist[w]);
+                                              sm.tab[w], sm.alist[w]);
   } else if (run < d.nruns1) {
     const StageWait wt{ctr - 1, (unsigned)(d.groups0 * BATCH_WARPS) + lim.extra, error,
                        lim.spins};
     bp_runs_warp<1, R, StageWait, false, FULL>(d.in, d.out, d.angles, d.g, run % d.g.SX,
-                                               (run / d.g.SX) * RUN, h, 1, sm.runs.tab[w],
-                                               sm.runs.alist[w], wt);
+                                               (run / d.g.SX) * RUN, h, 1, sm.tab[w],
+                                               sm.alist[w], wt);
   }
   signal_done(ctr);
 }
@@ -231,28 +241,73 @@ constexpr int batch_min_blocks(int body) {
 }
 
 template <int BODY>
+struct BodySmem {
+  using T = Bwd4Smem;
+};
+template <>
+struct BodySmem<B_FWD4> {
+  using T = FwdSmem;
+};
+template <>
+struct BodySmem<B_FWD8> {
+  using T = FwdSmem;
+};
+template <>
+struct BodySmem<B_FWD8F> {
+  using T = FwdSmem;
+};
+template <>
+struct BodySmem<B_BWD8> {
+  using T = RunsSmem;
+};
+template <>
+struct BodySmem<B_BWD8F> {
+  using T = RunsSmem;
+};
+
+__device__ __forceinline__ RunsSmem& runs_of(RunsSmem& sm) { return sm; }
+__device__ __forceinline__ RunsSmem& runs_of(Bwd4Smem& sm) { return sm.runs; }
+
+// Each block takes items from the body's counter; thread 0 finds the item's
+// problem and keeps its descriptor in shared memory, so the bodies read the
+// geometry from there instead of holding it in registers through the
+// gather.  Items are taken in increasing order, so a block's problem index
+// only moves forward and is looked up again only when the item leaves it.
+template <int BODY>
 __global__ void __launch_bounds__(BATCH_THREADS, batch_min_blocks(BODY))
     batch_kernel(const BatchDesc* __restrict__ descs, int ndesc, long long total,
                  unsigned long long* __restrict__ next, unsigned* __restrict__ counters,
                  int* __restrict__ error, WaitLimits lim) {
-  __shared__ BatchSmem sm;
+  __shared__ typename BodySmem<BODY>::T sm;
   __shared__ WaitSlot slots[BATCH_WARPS];
+  __shared__ BatchDesc s_desc;        // the current item's problem
   __shared__ long long s_item;
+  __shared__ long long s_next_begin;  // first item of the problem after s_desc's
+  __shared__ int s_lo;                // index of s_desc, -1: none yet
   const int w = threadIdx.x >> 5;
   const int lane = threadIdx.x & 31;
+  if (threadIdx.x == 0) s_lo = -1;
   for (;;) {
-    if (threadIdx.x == 0) s_item = (long long)atomicAdd(next, 1ull);
+    if (threadIdx.x == 0) {
+      const long long it = (long long)atomicAdd(next, 1ull);
+      s_item = it;
+      if (it < total && (s_lo < 0 || it >= s_next_begin)) {
+        int lo = s_lo < 0 ? 0 : s_lo, hi = ndesc - 1;
+        while (lo < hi) {
+          const int mid = (lo + hi + 1) >> 1;
+          if (descs[mid].begin <= it) lo = mid; else hi = mid - 1;
+        }
+        s_lo = lo;
+        s_desc = descs[lo];
+        s_next_begin = lo + 1 < ndesc ? descs[lo + 1].begin : total;
+      }
+    }
     __syncthreads();
     // the same for every lane: broadcast within the warp so that it is
     // warp-uniform to the compiler as well
     const long long item = __shfl_sync(0xffffffffu, s_item, 0);
     if (item >= total) return;  // block-uniform
-    int lo = 0, hi = ndesc - 1;
-    while (lo < hi) {
-      const int mid = (lo + hi + 1) >> 1;
-      if (descs[mid].begin <= item) lo = mid; else hi = mid - 1;
-    }
-    const BatchDesc d = descs[lo];
+    const BatchDesc& d = s_desc;
     // 32-bit index arithmetic: a problem's items fit in an int (checked when
     // the plan is made)
     const int local = (int)(item - d.begin);
@@ -264,20 +319,26 @@ __global__ void __launch_bounds__(BATCH_THREADS, batch_min_blocks(BODY))
       const int stage = in_chunk / per_stage;
       run_fwd_item<R, BODY == B_FWD8F>(d, stage, in_chunk - stage * per_stage, hc, sm,
                                        &slots[w], w, lane, counters, error, lim);
-    } else if (BODY == B_BWD8 || BODY == B_BWD8F || d.kind == K_BWD_RUNS) {
-      constexpr int R = (BODY == B_BWD8 || BODY == B_BWD8F) ? 8 : 4;
-      const bool first = in_chunk < d.groups0;
-      run_bwd_runs_item<R, BODY == B_BWD8F>(d, first ? 0 : 1,
-                                            first ? in_chunk : in_chunk - d.groups0, hc, sm, w,
-                                            lane, counters, error, lim);
     } else {
-      const int bidx = in_chunk * BATCH_WARPS + w;
-      if (bidx < d.nblocks)
-        bp_block_warp<2, 2>(d.in, d.out, d.angles, d.g, (bidx % d.nbx) * 2, (bidx / d.nbx) * 2,
-                            (hc * 32 + lane) * 4, 1,
-                            reinterpret_cast<float4(*)[4]>(&sm.blk.tw[w][0][0]), sm.blk.tb[w]);
+      // the adjoint bodies run faster on a register copy of the descriptor
+      // (108.3 against 110.6 ms on the 64-cube workload)
+      const BatchDesc dr = s_desc;
+      if (BODY == B_BWD8 || BODY == B_BWD8F || dr.kind == K_BWD_RUNS) {
+        constexpr int R = (BODY == B_BWD8 || BODY == B_BWD8F) ? 8 : 4;
+        const bool first = in_chunk < dr.groups0;
+        run_bwd_runs_item<R, BODY == B_BWD8F>(dr, first ? 0 : 1,
+                                              first ? in_chunk : in_chunk - dr.groups0, hc,
+                                              runs_of(sm), w, lane, counters, error, lim);
+      } else if constexpr (BODY == B_BWD4) {
+        const int bidx = in_chunk * BATCH_WARPS + w;
+        if (bidx < dr.nblocks)
+          bp_block_warp<2, 2>(dr.in, dr.out, dr.angles, dr.g, (bidx % dr.nbx) * 2,
+                              (bidx / dr.nbx) * 2, (hc * 32 + lane) * 4, 1,
+                              reinterpret_cast<float4(*)[4]>(&sm.blk.tw[w][0][0]),
+                              sm.blk.tb[w]);
+      }
     }
-    __syncthreads();  // shared memory and s_item are reused by the next item
+    __syncthreads();  // shared memory and the item are reused by the next item
   }
 }
 

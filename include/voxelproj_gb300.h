@@ -219,6 +219,18 @@ typedef struct vp_batch_plan vp_batch_plan;
 /* Validates the problems and uploads their descriptor table to the current
  * device (the only device allocation); *plan receives the plan. */
 VP_API int vp_batch_create(const vp_batch_problem* problems, int count, vp_batch_plan** plan);
+/* Re-plans `plan` for another set of problems (validated as by
+ * vp_batch_create), without synchronising the device: the descriptors go up
+ * by an asynchronous copy on `stream` from the plan's page-locked staging
+ * (two buffers used in turn; an update waits only for the upload of two
+ * updates before), and device buffers are reallocated in stream order only
+ * when the new set needs more room than the plan has.  Runs enqueued before
+ * on the same stream keep their problems, runs after see the new set: run
+ * the plan on the stream it was updated on, or order the two.  On an invalid
+ * problem the plan is left as it was.  For a scheduler whose set of problems
+ * changes from one step to the next.  No counterpart in the reference. */
+VP_API int vp_batch_update(vp_batch_plan* plan, const vp_batch_problem* problems, int count,
+                           void* stream);
 /* Enqueues the whole batch on `stream`: a counter reset and one persistent
  * launch per body present.  Allocates and synchronises nothing, so it can be
  * captured in a CUDA graph.  Runs of the same plan must not overlap on the

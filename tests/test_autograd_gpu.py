@@ -3,6 +3,8 @@
 * gradcheck in float64 at 16^3 with 8 angles (finite differences against the
   adjoint kernel's Jacobian; the operator is linear, so a large step costs no
   accuracy and keeps float32 rounding of the kernels small);
+* the gradients against the Jacobian of the FP64 operator from FP64 finite
+  differences, at the same size;
 * the gradient is the adjoint kernel's output, matches the FP64 oracle and
   the reference's recorded backward;
 * Adam, SIRT and CGLS reduce the data misfit.
@@ -37,6 +39,85 @@ def test_gradcheck_float64(z):
                    requires_grad=True)
     assert torch.autograd.gradcheck(lambda v: backproject(v, ang, (16, 16), z), (y,), eps=1e-2,
                                     atol=1e-3, rtol=1e-3)
+
+
+def fp64_jacobian(SY, SX, ang, PX, step=2.0 ** -4, seed=5):
+    """The Jacobian (n*PX, SY*SX) of the FP64 operator on one height plane, by
+    central finite differences in FP64 around a random float32 point.  Heights
+    are independent, so one oracle call evaluates every basis direction: height
+    j of the volume holds x0 + step * e_j (resp. - step).  x0 lies on a grid
+    of 1/256 and the step is 1/16, so the oracle's float32 input holds the
+    perturbed points exactly."""
+    ncols = SY * SX
+    # on a grid of 1/256, so that x0 +- step are float32 sums without rounding
+    x0 = (np.random.default_rng(seed).integers(0, 256, (SY, SX)) / 256.0).astype(np.float32)
+    E = np.eye(ncols, dtype=np.float32).reshape(ncols, SY, SX) * np.float32(step)
+    plus = np.ascontiguousarray((x0[None] + E).transpose(1, 2, 0))  # (SY, SX, ncols)
+    minus = np.ascontiguousarray((x0[None] - E).transpose(1, 2, 0))
+    fp = oracle.forward_f64(plus, ang, PX, 0)   # (ncols, n, PX)
+    fm = oracle.forward_f64(minus, ang, PX, 0)
+    J = (fp - fm) / (2.0 * step)
+    return J.reshape(ncols, -1).T  # (n*PX, ncols)
+
+
+@pytest.mark.parametrize("trig", ["precise", "reference"])
+@pytest.mark.parametrize("z", [0, 2])
+def test_gradients_match_fp64_finite_differences(z, trig):
+    """The spec check at the gradcheck size (16^3, 8 angles): the
+    gradients autograd returns, computed by the hand-written float32 kernels
+    (A^T for project, A for backproject), against the Jacobian of the FP64
+    operator obtained by FP64 finite differences.  Bound: the float32 error
+    of the chosen trig mode at this size (the Jacobian itself is exact up to
+    FP64 rounding, the operator being linear)."""
+    SY = SX = PX = 16
+    n, H = 8, 8
+    ang_np = lin(n)
+    J = fp64_jacobian(SY, SX, ang_np, PX)
+    rng = np.random.default_rng(17)
+    xin = rng.standard_normal((SY, SX, H)).astype(np.float32)
+    vin = rng.standard_normal((n, PX, H)).astype(np.float32)
+
+    def to_layout(a):  # z_order 0 array -> the z_order's layout
+        return np.ascontiguousarray(a if z == 0 else a.transpose(2, 0, 1))
+
+    ang = torch.tensor(ang_np, device="cuda")
+    vp.set_trig_mode(trig)
+    try:
+        # d<A x, v>/dx = A^T v
+        x = torch.tensor(to_layout(xin), device="cuda", requires_grad=True)
+        v = torch.tensor(to_layout(vin), device="cuda")
+        (project(x, ang, PX, z) * v).sum().backward()
+        gx = x.grad.cpu().numpy()
+        # d<A^T y, w>/dy = A w
+        y = torch.tensor(to_layout(vin), device="cuda", requires_grad=True)
+        w = torch.tensor(to_layout(xin), device="cuda")
+        (backproject(y, ang, (SY, SX), z) * w).sum().backward()
+        gy = y.grad.cpu().numpy()
+        torch.cuda.synchronize()
+    finally:
+        vp.set_trig_mode("reference")
+    if z == 2:
+        gx = gx.transpose(1, 2, 0)
+        gy = gy.transpose(1, 2, 0)
+    # FP64: per height, A^T v = J^T v_h and A w = J w_h
+    want_gx = np.stack([(J.T @ vin[:, :, h].astype(np.float64).ravel()).reshape(SY, SX)
+                        for h in range(H)], axis=-1)
+    want_gy = np.stack([(J @ xin[:, :, h].astype(np.float64).ravel()).reshape(n, PX)
+                        for h in range(H)], axis=-1)
+    ex, ey = rel_err(gx, want_gx), rel_err(gy, want_gy)
+    bound = tol.precise_vs_fp64(16) if trig == "precise" else tol.ref_vs_fp64(16)
+    print(f"\n[fd64] z={z} {trig}: grad of project {ex:.3e}, grad of backproject {ey:.3e}")
+    assert ex <= bound and ey <= bound
+
+
+def test_fp64_finite_difference_jacobian_is_the_oracle_operator():
+    """The finite-difference Jacobian reproduces the FP64 operator itself
+    (a check of the check): J u equals the oracle's A u in FP64."""
+    ang = lin(8)
+    J = fp64_jacobian(16, 16, ang, 16)
+    u = np.random.default_rng(3).standard_normal((16, 16, 1)).astype(np.float32)
+    Au = oracle.forward_f64(u, ang, 16, 0)[0].ravel()
+    assert np.abs(J @ u[:, :, 0].astype(np.float64).ravel() - Au).max() <= 1e-12 * np.abs(Au).max()
 
 
 def test_gradient_is_the_adjoint_kernel():

@@ -189,3 +189,57 @@ def test_autotuner_caches(tmp_path, monkeypatch):
     assert _lib.LIB.vp_get_kernel_variant(1) == vb
     _lib.LIB.vp_set_kernel_variant(1, 0)
     assert (tmp_path / "tune.json").exists()
+
+
+def test_batch_update_replans_in_place():
+    """vp_batch_update re-plans an existing plan for another set of problems:
+    a larger set (buffers grow), a smaller one, and a set with an invalid
+    problem (refused, plan unchanged).  Each run equals the single-problem
+    calls; runs enqueued before an update keep their problems."""
+    cases = _inputs(GEOMS, 300)
+
+    def make(sel):
+        probs, outs = [], []
+        for i in sel:
+            c = cases[i]
+            a = torch.tensor(c["ang"], device="cuda")
+            x = torch.tensor(c["x"], device="cuda")
+            y = torch.tensor(c["y"], device="cuda")
+            yo, xo = torch.zeros_like(y), torch.zeros_like(x)
+            probs += [("forward", x, yo, a), ("backward", y, xo, a)]
+            outs.append((x, y, a, yo, xo))
+        return probs, outs
+
+    def check(outs):
+        for x, y, a, yo, xo in outs:
+            ys, xs = torch.zeros_like(yo), torch.zeros_like(xo)
+            vp._CU.forward_z0(x, ys, a)
+            vp._CU.backward_z0(y, xs, a)
+            torch.cuda.synchronize()
+            assert torch.equal(yo, ys) and torch.equal(xo, xs)
+
+    p1, o1 = make([2])
+    b = Batch(p1)
+    b.run()                      # enqueued before the update: keeps problem 2
+    p2, o2 = make([0, 1, 2, 3])  # more problems than the plan was made for
+    b.update(p2)
+    b.run()
+    torch.cuda.synchronize()
+    check(o1)
+    check(o2)
+    p3, o3 = make([1])
+    b.update(p3)
+    b.run()
+    torch.cuda.synchronize()
+    check(o3)
+    bad = [("forward", p3[0][1], p3[0][2][:, :, :3].contiguous(), p3[0][3])]  # heights % 4
+    with pytest.raises(RuntimeError):
+        b.update(bad)
+    for _, _, _, yo, xo in o3:
+        yo.zero_()
+        xo.zero_()
+    b.run()                      # still the previous set
+    torch.cuda.synchronize()
+    check(o3)
+    assert not b.error()
+    b.close()

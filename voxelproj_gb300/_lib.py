@@ -72,6 +72,7 @@ SIGNATURES = {
     "vp_forward_z2_noalloc": (_I, [_P, _I64, _I64, _I64, _P, _I64, _I64, _I64, _P, _I64, _I,
                                    _P]),
     "vp_batch_create": (_I, [_P, _I, _P]),
+    "vp_batch_update": (_I, [_P, _P, _I, _P]),
     "vp_batch_run": (_I, [_P, _P]),
     "vp_batch_work_items": (_I64, [_P]),
     "vp_batch_error": (_I, [_P, _P]),

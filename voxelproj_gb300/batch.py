@@ -62,22 +62,40 @@ class Batch:
     """A fixed batch of projection problems (see the module docstring)."""
 
     def __init__(self, problems, device=None):
-        self._keep = []
-        probs = []
+        keep, arr, n = self._convert(problems)
+        self._keep = keep
+        self.device = torch.device(device) if device is not None else (
+            keep[0][0].device if keep else torch.device("cuda"))
+        self._plan = ctypes.c_void_p()
+        with torch.cuda.device(self.device):
+            _lib.check(_lib.LIB.vp_batch_create(arr, n, ctypes.byref(self._plan)),
+                       "batch_create")
+        self.work_items = int(_lib.LIB.vp_batch_work_items(self._plan))
+
+    @staticmethod
+    def _convert(problems):
+        keep, probs = [], []
         for spec in problems:
             op, inp, out, angles = spec[:4]
             variant = spec[4] if len(spec) > 4 else None
             if op not in _OPS:
                 raise KeyError(op)
             probs.append(_problem(op, inp, out, angles, variant))
-            self._keep.append((inp, out, angles))
-        self.device = torch.device(device) if device is not None else (
-            self._keep[0][0].device if self._keep else torch.device("cuda"))
+            keep.append((inp, out, angles))
         arr = (_lib.BatchProblem * max(1, len(probs)))(*probs)
-        self._plan = ctypes.c_void_p()
+        return keep, arr, len(probs)
+
+    def update(self, problems, stream=None):
+        """Replace the batch's problems (as given to the constructor) without
+        synchronising (``vp_batch_update``): the new descriptors go up on
+        `stream` (default: the current stream), after the runs already
+        enqueued there and before the runs enqueued next."""
+        keep, arr, n = self._convert(problems)
+        s = stream if stream is not None else torch.cuda.current_stream(self.device)
         with torch.cuda.device(self.device):
-            _lib.check(_lib.LIB.vp_batch_create(arr, len(probs), ctypes.byref(self._plan)),
-                       "batch_create")
+            _lib.check(_lib.LIB.vp_batch_update(self._plan, arr, n, s.cuda_stream),
+                       "batch_update")
+        self._keep = keep
         self.work_items = int(_lib.LIB.vp_batch_work_items(self._plan))
 
     def run(self, stream=None):

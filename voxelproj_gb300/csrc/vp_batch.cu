@@ -42,6 +42,7 @@
 #include <atomic>
 #include <cstdint>
 #include <cstring>
+#include <mutex>
 #include <new>
 #include <vector>
 
@@ -380,6 +381,17 @@ struct vp_batch_plan {
   int ndesc[vp::NBODIES] = {};
   long long items[vp::NBODIES] = {};
   int grid[vp::NBODIES] = {};
+  // room of the device buffers, and whether they came from the stream-ordered
+  // allocator (grown by vp_batch_update) rather than cudaMalloc
+  size_t desc_cap = 0, counter_cap = 0;
+  bool descs_async = false, counters_async = false;
+  // vp_batch_update: two page-locked staging buffers for descriptor uploads,
+  // used in turn, each with the event of its last upload
+  vp::BatchDesc* staging[2] = {nullptr, nullptr};
+  size_t staging_cap[2] = {0, 0};
+  cudaEvent_t uploaded[2] = {nullptr, nullptr};
+  bool upload_pending[2] = {false, false};
+  int next_staging = 0;
 };
 
 namespace {
@@ -494,6 +506,112 @@ int batch_desc(const vp_batch_problem& p, std::vector<vp::BatchDesc>* out) {
   return VP_OK;
 }
 
+// A plan's descriptors and bookkeeping for a set of problems: descriptors
+// grouped by body, items numbered from 0 within each body, a persistent
+// grid of one full wave per body present.
+struct Layout {
+  std::vector<vp::BatchDesc> descs;
+  int first[vp::NBODIES] = {};
+  int ndesc[vp::NBODIES] = {};
+  long long items[vp::NBODIES] = {};
+  int grid[vp::NBODIES] = {};
+  long long total = 0;
+  long long ncounters = 0;
+};
+
+// Resident blocks per SM of each body on the current device (cached).
+cudaError_t blocks_per_sm(int device, int (&per_sm)[vp::NBODIES], int* sms) {
+  static std::mutex mu;
+  static int cached[64][vp::NBODIES + 1];
+  static bool have[64] = {};
+  std::lock_guard<std::mutex> lock(mu);
+  if (device >= 0 && device < 64 && have[device]) {
+    for (int b = 0; b < vp::NBODIES; ++b) per_sm[b] = cached[device][b];
+    *sms = cached[device][vp::NBODIES];
+    return cudaSuccess;
+  }
+  cudaError_t e = cudaDeviceGetAttribute(sms, cudaDevAttrMultiProcessorCount, device);
+  for (int b = 0; b < vp::NBODIES && e == cudaSuccess; ++b)
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm[b], vp::batch_kernel_for(b),
+                                                      vp::BATCH_THREADS, 0);
+  if (e == cudaSuccess && device >= 0 && device < 64) {
+    for (int b = 0; b < vp::NBODIES; ++b) cached[device][b] = per_sm[b];
+    cached[device][vp::NBODIES] = *sms;
+    have[device] = true;
+  }
+  return e;
+}
+
+// Validates the problems and lays out their descriptors (no CUDA call).
+int make_layout(const vp_batch_problem* problems, int count, Layout* L) {
+  std::vector<vp::BatchDesc> by_body[vp::NBODIES];
+  std::vector<vp::BatchDesc> parts;
+  for (int i = 0; i < count; ++i) {
+    parts.clear();
+    if (int s = batch_desc(problems[i], &parts)) return s;
+    for (const vp::BatchDesc& d : parts) by_body[vp::body_of(d)].push_back(d);
+  }
+  L->descs.reserve(2 * (size_t)count);
+  for (int b = 0; b < vp::NBODIES; ++b) {
+    L->first[b] = (int)L->descs.size();
+    long long items = 0;
+    for (vp::BatchDesc d : by_body[b]) {
+      const long long n = d.begin;
+      d.begin = items;
+      items += n;
+      const long long nc = d.counter_base;
+      d.counter_base = (int)L->ncounters;
+      L->ncounters += nc;
+      L->descs.push_back(d);
+    }
+    L->ndesc[b] = (int)by_body[b].size();
+    L->items[b] = items;
+    L->total += items;
+  }
+  if (L->ncounters >= (1ll << 31)) return VP_ERR_BATCH;
+  return VP_OK;
+}
+
+// One full wave of blocks per body present, on `device`.
+int fill_grid(int device, Layout* L) {
+  int per_sm[vp::NBODIES] = {}, sms = 0;
+  const cudaError_t e = blocks_per_sm(device, per_sm, &sms);
+  if (e != cudaSuccess) return vp::record_cuda_error(e);
+  for (int b = 0; b < vp::NBODIES; ++b) {
+    if (L->items[b] == 0) continue;
+    const long long wave = (long long)sms * (per_sm[b] > 0 ? per_sm[b] : 1);
+    L->grid[b] = (int)(L->items[b] < wave ? L->items[b] : wave);
+  }
+  return VP_OK;
+}
+
+void adopt_layout(vp_batch_plan* pl, const Layout& L) {
+  for (int b = 0; b < vp::NBODIES; ++b) {
+    pl->first[b] = L.first[b];
+    pl->ndesc[b] = L.ndesc[b];
+    pl->items[b] = L.items[b];
+    pl->grid[b] = L.grid[b];
+  }
+  pl->total = L.total;
+  pl->ncounters = (int)L.ncounters;
+}
+
+// Grows a stream-ordered device buffer to at least `need` elements of `size`
+// bytes (by half again), freeing the old one in stream order.
+cudaError_t grow(void** buf, size_t* cap, bool* async, size_t need, size_t size,
+                 cudaStream_t st) {
+  if (need <= *cap) return cudaSuccess;
+  const size_t n = need + need / 2;
+  void* fresh = nullptr;
+  cudaError_t e = cudaMallocAsync(&fresh, n * size, st);
+  if (e != cudaSuccess) return e;
+  if (*buf) e = *async ? cudaFreeAsync(*buf, st) : cudaFree(*buf);
+  *buf = fresh;
+  *cap = n;
+  *async = true;
+  return e;
+}
+
 }  // namespace
 
 extern "C" {
@@ -502,54 +620,21 @@ int vp_batch_create(const vp_batch_problem* problems, int count, vp_batch_plan**
   if (plan == nullptr || (count > 0 && problems == nullptr)) return VP_ERR_NULL_POINTER;
   if (count < 0) return VP_ERR_BATCH;
   *plan = nullptr;
-  std::vector<vp::BatchDesc> descs;
-  descs.reserve(2 * (size_t)count);
-  // descriptors grouped by body; items numbered from 0 within each body
-  std::vector<vp::BatchDesc> by_body[vp::NBODIES];
-  std::vector<vp::BatchDesc> parts;
-  for (int i = 0; i < count; ++i) {
-    parts.clear();
-    if (int s = batch_desc(problems[i], &parts)) return s;
-    for (const vp::BatchDesc& d : parts) by_body[vp::body_of(d)].push_back(d);
-  }
+  Layout L;
+  if (int s = make_layout(problems, count, &L)) return s;
+  int device = 0;
+  cudaError_t e = cudaGetDevice(&device);
+  if (e != cudaSuccess) return vp::record_cuda_error(e);
+  if (int s = fill_grid(device, &L)) return s;
   vp_batch_plan* pl = new (std::nothrow) vp_batch_plan;
   if (pl == nullptr) return VP_ERR_BATCH;
-  long long ncounters = 0;
-  for (int b = 0; b < vp::NBODIES; ++b) {
-    pl->first[b] = (int)descs.size();
-    long long items = 0;
-    for (vp::BatchDesc d : by_body[b]) {
-      const long long n = d.begin;
-      d.begin = items;
-      items += n;
-      const long long nc = d.counter_base;
-      d.counter_base = (int)ncounters;
-      ncounters += nc;
-      descs.push_back(d);
-    }
-    pl->ndesc[b] = (int)by_body[b].size();
-    pl->items[b] = items;
-    pl->total += items;
-  }
-  if (ncounters >= (1ll << 31)) {
-    delete pl;
-    return VP_ERR_BATCH;
-  }
-  cudaError_t e = cudaGetDevice(&pl->device);
-  int sms = 0;
-  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, pl->device);
-  for (int b = 0; b < vp::NBODIES && e == cudaSuccess; ++b) {
-    if (pl->items[b] == 0) continue;
-    int per_sm = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, vp::batch_kernel_for(b),
-                                                      vp::BATCH_THREADS, 0);
-    const long long wave = (long long)sms * (per_sm > 0 ? per_sm : 1);
-    pl->grid[b] = (int)(pl->items[b] < wave ? pl->items[b] : wave);
-  }
-  if (e == cudaSuccess && !descs.empty())
-    e = cudaMalloc(&pl->d_descs, descs.size() * sizeof(vp::BatchDesc));
+  pl->device = device;
+  adopt_layout(pl, L);
+  const std::vector<vp::BatchDesc>& descs = L.descs;
+  if (!descs.empty()) e = cudaMalloc(&pl->d_descs, descs.size() * sizeof(vp::BatchDesc));
   if (e == cudaSuccess) e = cudaMalloc(&pl->d_next, vp::NBODIES * sizeof(unsigned long long));
-  if (e == cudaSuccess && ncounters > 0) e = cudaMalloc(&pl->d_counters, ncounters * sizeof(unsigned));
+  if (e == cudaSuccess && L.ncounters > 0)
+    e = cudaMalloc(&pl->d_counters, L.ncounters * sizeof(unsigned));
   if (e == cudaSuccess) e = cudaMalloc(&pl->d_error, sizeof(int));
   if (e == cudaSuccess && !descs.empty())
     e = cudaMemcpy(pl->d_descs, descs.data(), descs.size() * sizeof(vp::BatchDesc),
@@ -559,8 +644,53 @@ int vp_batch_create(const vp_batch_problem* problems, int count, vp_batch_plan**
     vp_batch_destroy(pl);
     return vp::record_cuda_error(e);
   }
-  pl->ncounters = (int)ncounters;
+  pl->desc_cap = descs.size();
+  pl->counter_cap = (size_t)L.ncounters;
   *plan = pl;
+  return VP_OK;
+}
+
+int vp_batch_update(vp_batch_plan* plan, const vp_batch_problem* problems, int count,
+                    void* stream) {
+  if (plan == nullptr || (count > 0 && problems == nullptr)) return VP_ERR_NULL_POINTER;
+  if (count < 0) return VP_ERR_BATCH;
+  Layout L;
+  if (int s = make_layout(problems, count, &L)) return s;  // plan unchanged
+  if (int s = fill_grid(plan->device, &L)) return s;
+  cudaStream_t st = (cudaStream_t)stream;
+  const size_t nd = L.descs.size();
+  cudaError_t e = grow(reinterpret_cast<void**>(&plan->d_descs), &plan->desc_cap,
+                       &plan->descs_async, nd, sizeof(vp::BatchDesc), st);
+  if (e == cudaSuccess)
+    e = grow(reinterpret_cast<void**>(&plan->d_counters), &plan->counter_cap,
+             &plan->counters_async, (size_t)L.ncounters, sizeof(unsigned), st);
+  if (e == cudaSuccess && nd > 0) {
+    // the staging buffer used two updates ago: wait for its upload to leave it
+    const int k = plan->next_staging;
+    plan->next_staging ^= 1;
+    if (plan->upload_pending[k]) e = cudaEventSynchronize(plan->uploaded[k]);
+    if (e == cudaSuccess && plan->uploaded[k] == nullptr)
+      e = cudaEventCreateWithFlags(&plan->uploaded[k], cudaEventDisableTiming);
+    if (e == cudaSuccess && plan->staging_cap[k] < nd) {
+      if (plan->staging[k]) e = cudaFreeHost(plan->staging[k]);
+      plan->staging[k] = nullptr;
+      plan->staging_cap[k] = 0;
+      const size_t n = nd + nd / 2;
+      if (e == cudaSuccess)
+        e = cudaMallocHost(reinterpret_cast<void**>(&plan->staging[k]),
+                           n * sizeof(vp::BatchDesc));
+      if (e == cudaSuccess) plan->staging_cap[k] = n;
+    }
+    if (e == cudaSuccess) {
+      std::memcpy(plan->staging[k], L.descs.data(), nd * sizeof(vp::BatchDesc));
+      e = cudaMemcpyAsync(plan->d_descs, plan->staging[k], nd * sizeof(vp::BatchDesc),
+                          cudaMemcpyHostToDevice, st);
+    }
+    if (e == cudaSuccess) e = cudaEventRecord(plan->uploaded[k], st);
+    if (e == cudaSuccess) plan->upload_pending[k] = true;
+  }
+  if (e != cudaSuccess) return vp::record_cuda_error(e);
+  adopt_layout(plan, L);
   return VP_OK;
 }
 
@@ -602,10 +732,19 @@ int vp_batch_destroy(vp_batch_plan* plan) {
   int prev = 0;
   cudaGetDevice(&prev);
   cudaSetDevice(plan->device);
-  if (plan->d_descs) cudaFree(plan->d_descs);
+  // buffers grown by vp_batch_update came from the stream-ordered allocator
+  if (plan->d_descs) plan->descs_async ? cudaFreeAsync(plan->d_descs, nullptr) : cudaFree(plan->d_descs);
   if (plan->d_next) cudaFree(plan->d_next);
-  if (plan->d_counters) cudaFree(plan->d_counters);
+  if (plan->d_counters)
+    plan->counters_async ? cudaFreeAsync(plan->d_counters, nullptr) : cudaFree(plan->d_counters);
   if (plan->d_error) cudaFree(plan->d_error);
+  for (int k = 0; k < 2; ++k) {
+    if (plan->uploaded[k]) {
+      cudaEventSynchronize(plan->uploaded[k]);
+      cudaEventDestroy(plan->uploaded[k]);
+    }
+    if (plan->staging[k]) cudaFreeHost(plan->staging[k]);
+  }
   cudaSetDevice(prev);
   delete plan;
   return VP_OK;

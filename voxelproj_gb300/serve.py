@@ -23,8 +23,11 @@ result does not depend on the other requests in the mix
 (tests/test_serve_gpu.py).
 
 The batches run on the persistent kernels of vp_batch_run
-(voxelproj_gb300.batch); their plans are cached per set of batched requests
-and rebuilt when the set changes.
+(voxelproj_gb300.batch): one plan per direction, re-planned in place
+(vp_batch_update, no synchronisation) when the set of batched requests
+changes.  A request's completion time is the GPU timestamp of a CUDA event
+recorded after its last step, read without blocking, so retiring requests
+does not stall the queue of work.
 
     python -m voxelproj_gb300.serve [--requests 24] [--rate 200]
 
@@ -124,7 +127,11 @@ class ReconstructionServer:
         self.active: list[_State] = []
         self.done: list[Request] = []
         self.in_use = 0
-        self._plans = {}
+        self._plans = {}      # direction -> Batch, re-planned in place
+        self._plan_keys = {}  # direction -> the set of requests it holds
+        self._pending = []    # (request, event after its last step)
+        self._ev0 = None      # CUDA event at the clock's reading _host0
+        self._host0 = 0.0
         self.ticks = 0
 
     # -- submission and admission ------------------------------------------
@@ -180,15 +187,37 @@ class ReconstructionServer:
 
     # -- batches ---------------------------------------------------------------
     def _plan(self, key, problems) -> Batch:
-        plan = self._plans.get(key)
+        tag = key[0]
+        plan = self._plans.get(tag)
         if plan is None:
-            if len(self._plans) > 8:
-                for b in self._plans.values():
-                    b.close()
-                self._plans.clear()
             plan = Batch(problems, device=self.device)
-            self._plans[key] = plan
+            self._plans[tag] = plan
+        elif self._plan_keys.get(tag) != key:
+            plan.update(problems)
+        self._plan_keys[tag] = key
         return plan
+
+    # -- completion times ------------------------------------------------------
+    def _mark_origin(self) -> None:
+        """Pairs a CUDA event with a reading of the clock (once)."""
+        if self._ev0 is None:
+            self._ev0 = torch.cuda.Event(enable_timing=True)
+            self._ev0.record()
+            torch.cuda.synchronize(self.device)
+            self._host0 = self.clock()
+
+    def _resolve(self, block: bool) -> None:
+        """Sets the completion time of retired requests whose last step is
+        done on the GPU (all of them with block)."""
+        if block and self._pending:
+            torch.cuda.synchronize(self.device)
+        left = []
+        for req, ev in self._pending:
+            if block or ev.query():
+                req.finished = self._host0 + self._ev0.elapsed_time(ev) / 1e3
+            else:
+                left.append((req, ev))
+        self._pending = left
 
     def _large(self, req: Request) -> bool:
         return (self.launch == "auto" and
@@ -234,6 +263,7 @@ class ReconstructionServer:
     # -- one tick ------------------------------------------------------------
     def step(self) -> None:
         """Admit, advance every active request by one iteration, retire."""
+        self._mark_origin()
         self._admit(self.clock())
         if not self.active:
             return
@@ -297,14 +327,15 @@ class ReconstructionServer:
             st.fresh = False
         finished = [st for st in self.active if st.done >= st.req.iters]
         if finished:
-            torch.cuda.synchronize(self.device)
-            now = self.clock()
+            ev = torch.cuda.Event(enable_timing=True)
+            ev.record()
             for st in finished:
                 st.req.x = st.bufs["x"]
-                st.req.finished = now
                 self.in_use -= st.req.footprint()
                 self.done.append(st.req)
+                self._pending.append((st.req, ev))
             self.active = [st for st in self.active if st.done < st.req.iters]
+        self._resolve(block=False)
 
     def idle(self) -> bool:
         return not self.active and not self.queue
@@ -320,9 +351,13 @@ class ReconstructionServer:
         return self.done
 
     def close(self) -> None:
+        """Waits for the GPU, sets the remaining completion times, frees the
+        plans."""
+        self._resolve(block=True)
         for b in self._plans.values():
             b.close()
         self._plans.clear()
+        self._plan_keys.clear()
 
 
 def solve_plain(req: Request) -> torch.Tensor:
@@ -363,8 +398,74 @@ def _latency_stats(reqs, origin):
             "solves_per_s": round(len(reqs) / span, 4), "makespan_s": round(span, 3)}
 
 
+def fill_table(sides=(32, 64, 96, 128, 192, 256, 384, 512), angles=(128, 1024), copies=16,
+               reps=3, device="cuda"):
+    """How much of the GPU one projection fills, by problem size: for cubes of
+    each side and angle count, A and A^T as single calls (GVU/s, and the
+    forward's blocks in waves of resident blocks), and `copies` such problems
+    (A and A^T each) in one batched launch per body, replayed as a CUDA graph,
+    against the same calls made one after another.  Returns one dict per
+    (side, angles)."""
+    from . import _CU
+
+    dev = torch.device(device)
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+
+    def timed(fn):
+        fn()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        for _ in range(reps):
+            fn()
+        b.record()
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / reps
+
+    rows = []
+    g = torch.Generator(device=dev).manual_seed(3)
+    for side in sides:
+        for n in angles:
+            ang = torch.linspace(0, np.pi, n + 1, device=dev)[:-1].contiguous()
+            xs = [torch.randn(side, side, side, device=dev, generator=g) for _ in range(copies)]
+            ys = [torch.zeros(n, side, side, device=dev) for _ in range(copies)]
+            xb = [torch.zeros(side, side, side, device=dev) for _ in range(copies)]
+            vu = float(side) ** 3 * n
+            t_a = timed(lambda: _CU.forward_z0(xs[0], ys[0], ang))
+            t_at = timed(lambda: _CU.backward_z0(ys[0], xb[0], ang))
+
+            def seq():
+                for i in range(copies):
+                    _CU.forward_z0(xs[i], ys[i], ang)
+                    _CU.backward_z0(ys[i], xb[i], ang)
+
+            batch = Batch([("forward", xs[i], ys[i], ang) for i in range(copies)]
+                          + [("backward", ys[i], xb[i], ang) for i in range(copies)], device=dev)
+            graph = batch.graph()
+            t_seq = timed(seq)
+            t_batch = timed(graph.replay)
+            batch.close()
+            # the forward's blocks: 16 bins x one angle x one chunk of heights
+            chunk = 256 if side > 128 else 128
+            blocks = -(-side // 16) * n * -(-side // chunk)
+            rows.append({
+                "side": side, "angles": n,
+                "A_ms": round(t_a, 4), "A_gvu_s": round(vu / t_a / 1e6, 1),
+                "AT_ms": round(t_at, 4), "AT_gvu_s": round(vu / t_at / 1e6, 1),
+                "forward_blocks_in_waves": round(blocks / (sms * 7), 2),
+                "copies": copies, "sequential_ms": round(t_seq, 3),
+                "batched_ms": round(t_batch, 3), "batch_gain": round(t_seq / t_batch, 3),
+            })
+            del xs, ys, xb
+            torch.cuda.empty_cache()
+    return rows
+
+
 def main() -> None:
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawTextHelpFormatter)
+    ap.add_argument("--fill", action="store_true",
+                    help="print, by problem size, how much of the GPU one projection fills "
+                         "and the gain of batching equal problems, then exit")
     ap.add_argument("--requests", type=int, default=24)
     ap.add_argument("--rate", type=float, default=200.0)
     ap.add_argument("--budget-gb", type=float, default=96.0)
@@ -380,8 +481,15 @@ def main() -> None:
     ap.add_argument("--warmup-s", type=float, default=10.0,
                     help="untimed projections before the timed phases (a fresh GPU "
                          "runs slower for its first tens of seconds under load)")
+    ap.add_argument("--min-angles", type=int, default=128)
+    ap.add_argument("--max-angles", type=int, default=1024)
     args = ap.parse_args()
-    reqs = make_requests(args.requests, args.rate, sides=(args.min_side, args.max_side))
+    if args.fill:
+        for row in fill_table():
+            print(json.dumps(row), flush=True)
+        return
+    reqs = make_requests(args.requests, args.rate, sides=(args.min_side, args.max_side),
+                         angles=(args.min_angles, args.max_angles))
     torch.cuda.synchronize()
 
     # warm-up: A and A^T on a mid-sized problem for warmup_s seconds
@@ -443,8 +551,9 @@ def main() -> None:
              for r in reqs)
     print(json.dumps({
         "workload": f"{args.requests} SIRT requests, Poisson {args.rate}/s, side "
-                    f"U{{{args.min_side}..{args.max_side}}}, angles U{{128..1024}}, "
-                    "iterations U{20..100}",
+                    f"U{{{args.min_side}..{args.max_side}}}, angles "
+                    f"U{{{args.min_angles}..{args.max_angles}}}, iterations U{{20..100}}",
+        "max_active": args.max_active,
         "served": served_stats, "plain_sequential": plain_stats,
         "plain_sequential_shortest_first": plain_sjf_stats,
         "solves_per_s_ratio": round(served_stats["solves_per_s"] / plain_stats["solves_per_s"], 3),

@@ -335,9 +335,11 @@ def run_ours(args, world, rank, local):
     if world > 1:
         torch.distributed.init_process_group("nccl", device_id=dev)
     vp.set_trig_mode(args.trig)
-    op_f, op_b = (0, 1) if args.z_order == 0 else (2, 3)
-    _lib.LIB.vp_set_kernel_variant(op_f, args.variant_fwd)
-    _lib.LIB.vp_set_kernel_variant(op_b, args.variant_bwd)
+    # z_order 2 with 32 heights or more runs the z_order 0 kernels between
+    # transposes: the variants apply to those too
+    for op_f, op_b in ((0, 1), (2, 3)) if args.z_order == 2 else ((0, 1),):
+        _lib.LIB.vp_set_kernel_variant(op_f, args.variant_fwd)
+        _lib.LIB.vp_set_kernel_variant(op_b, args.variant_bwd)
     S, n, z, H = args.size, args.angles, args.z_order, heights(args)
     PX = S
     xs, ys = shapes(S, n, z, H)

@@ -198,7 +198,8 @@ typedef struct vp_batch_problem {
   int flags;              /* VP_FLAG_* as for the single-problem calls */
   int variant;            /* the single-problem kernel variant whose body,
                              heights per lane and slabs the problem uses.
-                             Forward: 0 (default, = 10) or any variant with 4
+                             Forward: 0 (default: the single-problem
+                             default's slabs, = 11) or any variant with 4
                              bins per warp on neighbouring bins (1, 5, 7, 9,
                              10, 11, 12).  Adjoint: 0 / 7 = runs in two angle
                              classes, 8 heights per lane past 128 heights

@@ -406,8 +406,10 @@ int part_desc(const vp_batch_problem& p, const vp::Geom& g, const float* in, flo
   d->out = out;
   d->angles = p.angles;
   if (p.op == VP_OP_FORWARD) {
-    // the single-problem forward's plan for this variant (0: variant 10)
-    const vp::Fp0Plan pl = vp::forward_z0_plan(g, true, p.variant ? p.variant : 10);
+    // the single-problem forward's plan for this variant; 0: variant 11,
+    // the default's slabs and bodies without its angle groups (which the
+    // batch does not carry; they leave every sum unchanged)
+    const vp::Fp0Plan pl = vp::forward_z0_plan(g, true, p.variant ? p.variant : 11);
     if (pl.KW != 4 || pl.agroup || pl.split || pl.staged ||
         (pl.R == 8 ? pl.un != 2 : pl.un != vp::detail::FP0_UNROLL))
       return VP_ERR_BATCH;  // bodies the batch does not carry
@@ -488,7 +490,7 @@ int batch_desc(const vp_batch_problem& p, std::vector<vp::BatchDesc>* out) {
   // heights per lane of the first part
   int R = 4;
   if (fwd)
-    R = vp::forward_z0_plan(g, true, p.variant ? p.variant : 10).R;
+    R = vp::forward_z0_plan(g, true, p.variant ? p.variant : 11).R;
   else if ((p.variant == 0 || p.variant == 7) && H > 128)
     R = 8;
   const int H8 = R == 8 ? vp::r8_heights(g.H) : g.H;

@@ -222,20 +222,24 @@ struct Fp0Config {
 // neighbouring angles; 4 = 8 bins, neighbouring angles; 5 = 4 bins, 8
 // heights per lane, 2 candidates in flight; 6 = as 5 with 4 in flight;
 // 7 = as 5 with 64 MB slabs; 8 = 8 bins, 8 heights per lane; 9 / 10 / 11 =
-// as 5 with class slabs of 32 / 64 / 128 MB (10 is the default: 11 runs 1%
-// faster at 512^3 with 192 angles but misses L2 on the volume, 5.3 against
-// 4.6 GB of DRAM traffic per call); 12 = as 1
+// as 5 with class slabs of 32 / 64 / 128 MB; 12 = as 1
 // with class slabs of 32 MB; 13 = as 10 with two warps per bin run, each on
 // half of the slab's major lines (SPLIT); 14 / 15 = as 10 / 11 with 3
 // candidates in flight at 6 blocks per SM; 16 = as 10 with the warps of a
 // block on neighbouring angles; 17 = as 10, four aligned neighbouring angles
 // per block, the volume staged through shared memory by tensor copies
-// (vp_fp_staged.cuh); 19 = the aligned angle groups with plain loads.  Heights not in float4 run the scalar form of
+// (vp_fp_staged.cuh); 19 = the aligned angle groups with plain loads; 21 =
+// as 16 with 128 MB slabs.  The default (0) is 21 with 8 heights per lane
+// and 10's layout (neighbouring bins) in the 4-height form.  Measured A per
+// call, variants 10 / 21: 512^3 and 192 angles 7.167 / 6.950 ms; 1024
+// angles 35.46 / 34.30 ms; 256^3 and 360 angles 1.685 / 1.583 ms; 384^3
+// and 641 angles 10.71 / 10.67 ms.  Heights not in float4 run the scalar form of
 // the same bin layout; 8-height variants on problems of at most 128 heights
 // run the 4-height form.
 Fp0Config fp0_config(const Geom& g, bool vec4, int variant) {
   Fp0Config c{vec4 ? 4 : 1, 4, false, FP0_UNROLL, 32, false, false, 0};
-  if (variant == 0) variant = 10;  // the default
+  const bool dflt = variant == 0;
+  if (dflt) variant = 21;  // the default
   switch (variant) {
     case 2: c.KW = 8; break;
     case 3: c.agroup = true; break;
@@ -254,12 +258,17 @@ Fp0Config fp0_config(const Geom& g, bool vec4, int variant) {
     case 16: c.R = 8; c.un = 2; c.cls = true; c.slab_mb = 64; c.agroup = true; break;
     case 17: c.R = 8; c.un = 2; c.cls = true; c.slab_mb = 64; c.staged = 1; break;
     case 19: c.R = 8; c.un = 2; c.cls = true; c.slab_mb = 64; c.staged = 2; break;
+    case 21: c.R = 8; c.un = 2; c.cls = true; c.slab_mb = 128; c.agroup = true; break;
     default: break;
   }
   if (c.R == 8 && (!vec4 || g.H <= 128)) {
     c.R = vec4 ? 4 : 1;
     c.un = FP0_UNROLL;
     c.staged = 0;
+    // the default's 4-height form keeps neighbouring bins per block: angle
+    // groups measured slower there (128^3, 192 angles: 0.223 against
+    // 0.2095 ms)
+    if (dflt) c.agroup = false;
   }
   return c;
 }

@@ -198,10 +198,9 @@ typedef struct vp_batch_problem {
   int flags;              /* VP_FLAG_* as for the single-problem calls */
   int variant;            /* the single-problem kernel variant whose body,
                              heights per lane and slabs the problem uses.
-                             Forward: 0 (default: the single-problem
-                             default's slabs, = 11) or any variant with 4
-                             bins per warp on neighbouring bins (1, 5, 7, 9,
-                             10, 11, 12).  Adjoint: 0 / 7 = runs in two angle
+                             Forward: 0 (the single-problem default) or
+                             any variant with 4 bins per warp (1, 3, 5, 7, 9,
+                             10, 11, 12, 16, 21).  Adjoint: 0 / 7 = runs in two angle
                              classes, 8 heights per lane past 128 heights
                              (default); 6 = runs, 4 heights per lane; 4 = 2x2
                              voxel blocks (accumulates in the reference's

@@ -30,7 +30,8 @@ def _inputs(geoms, seed):
     return out
 
 
-@pytest.mark.parametrize("vf,vb", [(1, 4), (1, 6), (0, 0), (10, 7), (5, 6), (12, 7)])
+@pytest.mark.parametrize("vf,vb", [(1, 4), (1, 6), (0, 0), (10, 7), (5, 6), (12, 7), (21, 7),
+                                   (16, 6), (3, 4)])
 def test_batch_matches_single_problem_calls(vf, vb):
     """Same bodies, same slabs and stages, same order: the batch reproduces the
     single-problem kernels of the same variant bit for bit."""

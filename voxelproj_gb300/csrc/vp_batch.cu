@@ -84,9 +84,11 @@ struct BatchDesc {
   int R;                // heights per lane: 4, or 8 as two float4 128 apart
   int nstages;          // stages per chunk
   int counter_base;     // first counter of this problem (forward: per tile; adjoints: per stage)
-  // forward: slab plan (class slabs, rows and columns per slab), bin groups
-  // per angle
-  int cls, wy, wx, units;
+  // forward: slab plan (class slabs, rows and columns per slab); an item
+  // row is an angle (its bins in groups of 4 runs, one per warp) or, with
+  // agroup, a group of 4 neighbouring angles (one per warp, on the same
+  // 4-bin run); units: item columns per row
+  int cls, wy, wx, units, agroup, rows;
   // run adjoint: runs and run groups of each class
   int nruns0, groups0, nruns1, groups1;
   // block adjoint: blocks along x, blocks, block groups
@@ -160,9 +162,11 @@ __device__ __forceinline__ void signal_done(unsigned* counter) {
   }
 }
 
-// A forward item's outputs are the bins of one (height chunk, angle, bin
-// group) tile, written by one item per stage; its counter counts the warps
-// done on the tile, so a stage waits for the tile's previous stage alone.
+// A forward item's outputs are one (height chunk, item row, item column)
+// tile: 16 neighbouring bins of one angle, or with agroup 4 neighbouring bins
+// of 4 neighbouring angles; one item per stage writes it.  Its counter counts
+// the warps done on the tile, so a stage waits for the tile's previous stage
+// alone.
 // FULL: the part's heights are whole 256-height chunks (R = 8).
 // Out of line: its own register allocation, apart from the persistent loop's
 // state (on the 64-cube workload the batched forward took 169.8 against
@@ -173,15 +177,17 @@ __device__ __noinline__ void run_fwd_item(const BatchDesc& d, int stage, int in_
                                              int lane, unsigned* counters, int* error,
                                              const WaitLimits& lim) {
   constexpr int UN = R == 8 ? 2 : FP0_UNROLL;  // as the single-problem kernels
-  const int a = in_stage / d.units;
-  const int bg = in_stage - a * d.units;
+  const int row = in_stage / d.units;
+  const int u = in_stage - row * d.units;
   const Slab slab = slab_of(stage, d.cls, d.wy, d.wx, d.g.SY, d.g.SX);
+  // one counter per item tile: its 4 warps count themselves done on it
   if (lane == 0)
-    *slot = WaitSlot{counters + d.counter_base + ((size_t)hc * d.g.n_ang + a) * d.units + bg,
+    *slot = WaitSlot{counters + d.counter_base + ((size_t)hc * d.rows + row) * d.units + u,
                      error, stage > 0 ? (unsigned)(stage * BATCH_WARPS) + lim.extra : 0u,
                      lim.spins};
   __syncwarp();
-  const int p0 = (bg * BATCH_WARPS + w) * 4;
+  const int a = d.agroup ? row * BATCH_WARPS + w : row;
+  const int p0 = d.agroup ? u * 4 : (u * BATCH_WARPS + w) * 4;
   const int h = hc * 32 * R + lane * 4;
   fp_z0_warp<R, 4, UN, SlotWait, FULL>(d.in, d.out, d.angles, d.g, p0, a, h, slab, 1,
                                        sm.cand[w], SlotWait{slot});
@@ -316,7 +322,7 @@ __global__ void __launch_bounds__(BATCH_THREADS, batch_min_blocks(BODY))
     const int in_chunk = local - hc * (int)d.per_chunk;
     if constexpr (BODY == B_FWD4 || BODY == B_FWD8 || BODY == B_FWD8F) {
       constexpr int R = BODY == B_FWD4 ? 4 : 8;
-      const int per_stage = d.g.n_ang * d.units;
+      const int per_stage = d.rows * d.units;
       const int stage = in_chunk / per_stage;
       run_fwd_item<R, BODY == B_FWD8F>(d, stage, in_chunk - stage * per_stage, hc, sm,
                                        &slots[w], w, lane, counters, error, lim);
@@ -406,11 +412,9 @@ int part_desc(const vp_batch_problem& p, const vp::Geom& g, const float* in, flo
   d->out = out;
   d->angles = p.angles;
   if (p.op == VP_OP_FORWARD) {
-    // the single-problem forward's plan for this variant; 0: variant 11,
-    // the default's slabs and bodies without its angle groups (which the
-    // batch does not carry; they leave every sum unchanged)
-    const vp::Fp0Plan pl = vp::forward_z0_plan(g, true, p.variant ? p.variant : 11);
-    if (pl.KW != 4 || pl.agroup || pl.split || pl.staged ||
+    // the single-problem forward's plan for this variant (0: its default)
+    const vp::Fp0Plan pl = vp::forward_z0_plan(g, true, p.variant);
+    if (pl.KW != 4 || pl.split || pl.staged ||
         (pl.R == 8 ? pl.un != 2 : pl.un != vp::detail::FP0_UNROLL))
       return VP_ERR_BATCH;  // bodies the batch does not carry
     d->kind = vp::K_FWD;
@@ -419,8 +423,10 @@ int part_desc(const vp_batch_problem& p, const vp::Geom& g, const float* in, flo
     d->wy = pl.wy;
     d->wx = pl.wx;
     d->nstages = pl.nslabs;
-    d->units = (int)vp::ceil_div_u(g.PX, 4ll * vp::BATCH_WARPS);
-    d->per_chunk = (long long)d->nstages * g.n_ang * d->units;
+    d->agroup = pl.agroup ? 1 : 0;
+    d->rows = pl.agroup ? (int)vp::ceil_div_u(g.n_ang, vp::BATCH_WARPS) : g.n_ang;
+    d->units = (int)vp::ceil_div_u(g.PX, pl.agroup ? 4ll : 4ll * vp::BATCH_WARPS);
+    d->per_chunk = (long long)d->nstages * d->rows * d->units;
   } else if (p.variant == 0 || p.variant == 6 || p.variant == 7) {
     d->kind = vp::K_BWD_RUNS;
     d->R = R;
@@ -448,7 +454,7 @@ int part_desc(const vp_batch_problem& p, const vp::Geom& g, const float* in, flo
   d->begin = hch * d->per_chunk;  // item count, turned into offsets later
   // counter count, turned into offsets later: one per forward tile, one per
   // stage of the adjoints
-  const long long nctr = d->kind == vp::K_FWD ? hch * g.n_ang * d->units : hch * d->nstages;
+  const long long nctr = d->kind == vp::K_FWD ? hch * d->rows * d->units : hch * d->nstages;
   if (nctr >= (1ll << 31)) return VP_ERR_BATCH;
   d->counter_base = (int)nctr;
   return VP_OK;
@@ -490,7 +496,7 @@ int batch_desc(const vp_batch_problem& p, std::vector<vp::BatchDesc>* out) {
   // heights per lane of the first part
   int R = 4;
   if (fwd)
-    R = vp::forward_z0_plan(g, true, p.variant ? p.variant : 11).R;
+    R = vp::forward_z0_plan(g, true, p.variant).R;
   else if ((p.variant == 0 || p.variant == 7) && H > 128)
     R = 8;
   const int H8 = R == 8 ? vp::r8_heights(g.H) : g.H;

@@ -27,7 +27,7 @@ import torch
 
 from . import _lib
 
-BATCH_CANDIDATES = {"forward": [10, 11, 1], "backward": [7, 6, 4]}
+BATCH_CANDIDATES = {"forward": [21, 11, 10, 1], "backward": [7, 6, 4]}
 SINGLE_CANDIDATES = {"forward": [21, 10, 11, 16, 13, 7, 1], "backward": [7, 6, 4, 1]}
 TUNE_ANGLES = 90
 

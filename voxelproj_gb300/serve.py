@@ -481,6 +481,9 @@ def main() -> None:
     ap.add_argument("--warmup-s", type=float, default=10.0,
                     help="untimed projections before the timed phases (a fresh GPU "
                          "runs slower for its first tens of seconds under load)")
+    ap.add_argument("--warmup-requests", type=int, default=32,
+                    help="untimed stream of the same mix (2-4 iterations each) through the "
+                         "server and the plain solver before the timed phases")
     ap.add_argument("--min-angles", type=int, default=128)
     ap.add_argument("--max-angles", type=int, default=1024)
     args = ap.parse_args()
@@ -505,6 +508,28 @@ def main() -> None:
             _CU.backward_z0(wy, wx, wa)
             torch.cuda.synchronize()
         del wx, wy, wa
+
+    # warm-up stream: the same mix, few iterations, through both paths, so
+    # that first-use costs fall outside the timed phases.  On a fresh machine
+    # the first process to run this comparison measured the server at 0.91x
+    # of plain calls and every later one at 3.03x (same build, 32-64 sides at
+    # 2000/s): the first use of each element-wise op the server applies costs
+    # time once per machine.
+    if args.warmup_requests > 0:
+        wreqs = make_requests(args.warmup_requests, args.rate, seed=1011,
+                              sides=(args.min_side, args.max_side),
+                              angles=(args.min_angles, args.max_angles), iters=(2, 4))
+        wsrv = ReconstructionServer(int(args.budget_gb * 2**30), args.max_active,
+                                    policy=args.policy, launch=args.launch)
+        tw = time.perf_counter()
+        wsrv.clock = lambda: time.perf_counter() - tw
+        for r in wreqs:
+            wsrv.submit(r)
+        wsrv.run()
+        for r in wreqs[:4]:
+            solve_plain(r)
+        torch.cuda.synchronize()
+        del wreqs, wsrv
 
     # every phase starts with torch's allocator cache empty, so none reuses
     # the blocks another phase allocated

@@ -27,37 +27,65 @@ namespace {
 
 constexpr int TT = 32;         // tile edge
 constexpr int TROWS = 8;       // thread rows per tile (each thread moves TT/TROWS elements)
+constexpr int TPI = 2;         // tiles per block iteration
+constexpr int KE = TT / TROWS;
 
 // dst[c * dst_ld + r] (+)= src[r * src_ld + c] for r < rows, c < cols.
 // Tiles are visited with a grid-stride loop so any matrix fits one launch.
+// Each iteration moves TPI neighbouring tiles and issues every load of them
+// (the source rows into shared memory and, when adding, the destination's
+// current values into registers) before the first store: 16 loads in flight
+// per thread.  With the loads of one element's read-add-write in turn, the
+// adding launches waited on each destination read (57% of the copy
+// bandwidth against 65-68% for the storing ones).
 __global__ void __launch_bounds__(TT * TROWS)
     transpose_kernel(const float* __restrict__ src, float* __restrict__ dst, long long rows,
                      long long cols, long long src_ld, long long dst_ld, int accumulate) {
-  __shared__ float tile[TT][TT + 1];
+  __shared__ float tile[TPI][TT][TT + 1];
   const long long tiles_c = (cols + TT - 1) / TT;
   const long long tiles_r = (rows + TT - 1) / TT;
   const long long ntiles = tiles_c * tiles_r;
-  for (long long t = blockIdx.x; t < ntiles; t += gridDim.x) {
-    const long long r0 = (t / tiles_c) * TT;
-    const long long c0 = (t % tiles_c) * TT;
-    __syncthreads();
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  for (long long t0 = (long long)blockIdx.x * TPI; t0 < ntiles;
+       t0 += (long long)gridDim.x * TPI) {
+    float old[TPI][KE];
 #pragma unroll
-    for (int i = 0; i < TT; i += TROWS) {
-      const long long r = r0 + threadIdx.y + i;
-      const long long c = c0 + threadIdx.x;
-      if (r < rows && c < cols) tile[threadIdx.y + i][threadIdx.x] = __ldg(src + r * src_ld + c);
-    }
-    __syncthreads();
+    for (int j = 0; j < TPI; ++j) {
+      const long long t = t0 + j;
+      const long long r0 = (t / tiles_c) * TT;
+      const long long c0 = (t % tiles_c) * TT;
+      const bool tv = t < ntiles;
 #pragma unroll
-    for (int i = 0; i < TT; i += TROWS) {
-      const long long c = c0 + threadIdx.y + i;
-      const long long r = r0 + threadIdx.x;
-      if (r < rows && c < cols) {
-        float* p = dst + c * dst_ld + r;
-        const float v = tile[threadIdx.x][threadIdx.y + i];
-        *p = accumulate ? *p + v : v;
+      for (int k = 0; k < KE; ++k) {
+        const long long r = r0 + ty + k * TROWS;
+        const long long c = c0 + tx;
+        if (tv && r < rows && c < cols) tile[j][ty + k * TROWS][tx] = __ldg(src + r * src_ld + c);
+      }
+#pragma unroll
+      for (int k = 0; k < KE; ++k) {
+        const long long c = c0 + ty + k * TROWS;
+        const long long r = r0 + tx;
+        old[j][k] = (accumulate && tv && r < rows && c < cols) ? dst[c * dst_ld + r] : 0.0f;
       }
     }
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < TPI; ++j) {
+      const long long t = t0 + j;
+      const long long r0 = (t / tiles_c) * TT;
+      const long long c0 = (t % tiles_c) * TT;
+      const bool tv = t < ntiles;
+#pragma unroll
+      for (int k = 0; k < KE; ++k) {
+        const long long c = c0 + ty + k * TROWS;
+        const long long r = r0 + tx;
+        if (tv && r < rows && c < cols) {
+          const float v = tile[j][tx][ty + k * TROWS];
+          dst[c * dst_ld + r] = accumulate ? old[j][k] + v : v;
+        }
+      }
+    }
+    __syncthreads();  // the tiles are refilled next iteration
   }
 }
 
@@ -65,11 +93,17 @@ cudaError_t transpose(const float* src, float* dst, long long rows, long long co
                       long long src_ld, long long dst_ld, int accumulate, cudaStream_t stream) {
   if (rows <= 0 || cols <= 0) return cudaSuccess;
   const long long ntiles = ((rows + TT - 1) / TT) * ((cols + TT - 1) / TT);
-  int dev = 0, sms = 152;
+  const long long iters = (ntiles + TPI - 1) / TPI;
+  // one resident wave of blocks (the tiles are dealt out by block index)
+  int dev = 0, sms = 152, per_sm = 0;
   if (cudaGetDevice(&dev) == cudaSuccess)
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  const long long cap = (long long)sms * 8;
-  const unsigned grid = (unsigned)(ntiles < cap ? ntiles : cap);
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, transpose_kernel, TT * TROWS, 0) !=
+          cudaSuccess ||
+      per_sm < 1)
+    per_sm = 1;
+  const long long cap = (long long)sms * per_sm;
+  const unsigned grid = (unsigned)(iters < cap ? iters : cap);
   transpose_kernel<<<grid, dim3(TT, TROWS), 0, stream>>>(src, dst, rows, cols, src_ld, dst_ld,
                                                         accumulate);
   return cudaGetLastError();

@@ -239,10 +239,12 @@ __host__ __device__ inline int body_of(const BatchDesc& d) {
 // Resident blocks per SM the registers must allow, so that each body keeps
 // its single-problem kernel's occupancy despite the item bookkeeping:
 // 8-height forwards 7 (72 registers, a few spilled; at 6 blocks the 64-cube
-// batch took 332 ms instead of 322), 4-height forward 7 (72), 8-height run
-// adjoints 5 (96); the 4-height adjoints as the compiler chooses (72).
+// batch took 332 ms instead of 322), 4-height forward 8 (64, as the
+// single-problem 4-height kernel; at 7 blocks and 72 registers it ran 1.7%
+// slower than its single calls), 8-height run adjoints 5 (96); the 4-height
+// adjoints as the compiler chooses (72).
 constexpr int batch_min_blocks(int body) {
-  return (body == B_FWD8 || body == B_FWD8F || body == B_FWD4) ? 7
+  return body == B_FWD4 ? 8 : (body == B_FWD8 || body == B_FWD8F) ? 7
          : (body == B_BWD8 || body == B_BWD8F)                  ? 5
                                                                 : 0;
 }

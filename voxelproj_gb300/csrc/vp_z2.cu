@@ -27,20 +27,22 @@ namespace {
 
 constexpr int TT = 32;         // tile edge
 constexpr int TROWS = 8;       // thread rows per tile (each thread moves TT/TROWS elements)
-constexpr int TPI = 2;         // tiles per block iteration
 constexpr int KE = TT / TROWS;
 
 // dst[c * dst_ld + r] (+)= src[r * src_ld + c] for r < rows, c < cols.
 // Tiles are visited with a grid-stride loop so any matrix fits one launch.
-// Each iteration moves TPI neighbouring tiles and issues every load of them
-// (the source rows into shared memory and, when adding, the destination's
-// current values into registers) before the first store: 16 loads in flight
-// per thread.  With the loads of one element's read-add-write in turn, the
-// adding launches waited on each destination read (57% of the copy
-// bandwidth against 65-68% for the storing ones).
+// ADD: add into dst.  The adding form moves two neighbouring tiles per
+// iteration and issues every load of them (the source rows into shared
+// memory, the destination's current values into registers) before the first
+// store: 16 loads in flight per thread.  With one element's read-add-write
+// in turn it waited on each destination read (57% of the copy bandwidth
+// against 65-68% for the storing form, which keeps one tile per iteration,
+// 32 registers and 8 blocks per SM).
+template <bool ADD>
 __global__ void __launch_bounds__(TT * TROWS)
     transpose_kernel(const float* __restrict__ src, float* __restrict__ dst, long long rows,
-                     long long cols, long long src_ld, long long dst_ld, int accumulate) {
+                     long long cols, long long src_ld, long long dst_ld) {
+  constexpr int TPI = ADD ? 2 : 1;  // tiles per iteration
   __shared__ float tile[TPI][TT][TT + 1];
   const long long tiles_c = (cols + TT - 1) / TT;
   const long long tiles_r = (rows + TT - 1) / TT;
@@ -49,6 +51,7 @@ __global__ void __launch_bounds__(TT * TROWS)
   for (long long t0 = (long long)blockIdx.x * TPI; t0 < ntiles;
        t0 += (long long)gridDim.x * TPI) {
     float old[TPI][KE];
+    (void)old;
 #pragma unroll
     for (int j = 0; j < TPI; ++j) {
       const long long t = t0 + j;
@@ -65,7 +68,7 @@ __global__ void __launch_bounds__(TT * TROWS)
       for (int k = 0; k < KE; ++k) {
         const long long c = c0 + ty + k * TROWS;
         const long long r = r0 + tx;
-        old[j][k] = (accumulate && tv && r < rows && c < cols) ? dst[c * dst_ld + r] : 0.0f;
+        if constexpr (ADD) old[j][k] = (tv && r < rows && c < cols) ? dst[c * dst_ld + r] : 0.0f;
       }
     }
     __syncthreads();
@@ -81,7 +84,8 @@ __global__ void __launch_bounds__(TT * TROWS)
         const long long r = r0 + tx;
         if (tv && r < rows && c < cols) {
           const float v = tile[j][tx][ty + k * TROWS];
-          dst[c * dst_ld + r] = accumulate ? old[j][k] + v : v;
+          if constexpr (ADD) dst[c * dst_ld + r] = old[j][k] + v;
+          else dst[c * dst_ld + r] = v;
         }
       }
     }
@@ -93,19 +97,24 @@ cudaError_t transpose(const float* src, float* dst, long long rows, long long co
                       long long src_ld, long long dst_ld, int accumulate, cudaStream_t stream) {
   if (rows <= 0 || cols <= 0) return cudaSuccess;
   const long long ntiles = ((rows + TT - 1) / TT) * ((cols + TT - 1) / TT);
-  const long long iters = (ntiles + TPI - 1) / TPI;
+  const long long iters = accumulate ? (ntiles + 1) / 2 : ntiles;
   // one resident wave of blocks (the tiles are dealt out by block index)
   int dev = 0, sms = 152, per_sm = 0;
   if (cudaGetDevice(&dev) == cudaSuccess)
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, transpose_kernel, TT * TROWS, 0) !=
-          cudaSuccess ||
+  const void* fn = accumulate ? reinterpret_cast<const void*>(transpose_kernel<true>)
+                              : reinterpret_cast<const void*>(transpose_kernel<false>);
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, TT * TROWS, 0) != cudaSuccess ||
       per_sm < 1)
     per_sm = 1;
   const long long cap = (long long)sms * per_sm;
   const unsigned grid = (unsigned)(iters < cap ? iters : cap);
-  transpose_kernel<<<grid, dim3(TT, TROWS), 0, stream>>>(src, dst, rows, cols, src_ld, dst_ld,
-                                                        accumulate);
+  if (accumulate)
+    transpose_kernel<true><<<grid, dim3(TT, TROWS), 0, stream>>>(src, dst, rows, cols, src_ld,
+                                                                 dst_ld);
+  else
+    transpose_kernel<false><<<grid, dim3(TT, TROWS), 0, stream>>>(src, dst, rows, cols, src_ld,
+                                                                  dst_ld);
   return cudaGetLastError();
 }
 

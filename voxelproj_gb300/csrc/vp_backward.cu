@@ -17,6 +17,7 @@
 #include <cudaTypedefs.h>
 
 #include <atomic>
+#include <type_traits>
 
 #include "vp_bp_block.cuh"
 #include "vp_bp_runs.cuh"
@@ -159,7 +160,10 @@ __global__ void __launch_bounds__(32 * BPB_WARPS)
 // saw no angle of its class leaves x untouched (in store mode the first launch
 // always writes).
 // ---------------------------------------------------------------------------
-template <int PASS, int R, bool ADD = false, bool FULL = false>
+// PDL: the launch follows another run launch of the same call
+// programmatically (launch_ex), so its warps wait for that launch before they
+// add into x; a call's first launch keeps the form without the wait.
+template <int PASS, int R, bool ADD = false, bool FULL = false, bool PDL = false>
 __global__ void __launch_bounds__(32 * BPR_WARPS, R == 8 ? 5 : 0)
     bp_z0_runs_kernel(const float* __restrict__ y, float* __restrict__ x,
                       const float* __restrict__ angles, Geom g, int nrun_major, int run_base,
@@ -170,13 +174,23 @@ __global__ void __launch_bounds__(32 * BPR_WARPS, R == 8 ? 5 : 0)
   const int lane = threadIdx.x;
   const int w = threadIdx.y;
   const int run = run_base + blockIdx.x * BPR_WARPS + w;
+  // A programmatic launch of the next class may start as this one's last
+  // blocks run; each warp waits for the launch before it only to add its
+  // sums into x.  Warp 0 of every block has a run inside the range (the grid
+  // covers [run_base, run_end) in blocks of 4 runs, and a block's first run,
+  // or its band's first row, lies below row_end), so every block waits
+  // before it ends.  (Waits
+  // on the early returns below cost the 8-height form a register spill and
+  // 4% of its time.)
+  pdl_trigger();
   if (run >= run_end) return;  // warp-uniform; all shared state is per warp
   int xi0, yi0;
   run_origin<PASS>(run, nrun_major, &xi0, &yi0);
   if (yi0 >= row_end) return;
-  bp_runs_warp<PASS, R, NoWait, ADD, FULL>(y, x, angles, g, xi0, yi0,
-                                           blockIdx.y * 32 * R + lane * 4, accumulate, tab[w],
-                                           alist[w], NoWait(), addend);
+  using Wait = std::conditional_t<PDL, PdlWait, NoWait>;
+  bp_runs_warp<PASS, R, Wait, ADD, FULL>(y, x, angles, g, xi0, yi0,
+                                         blockIdx.y * 32 * R + lane * 4, accumulate, tab[w],
+                                         alist[w], Wait(), addend);
 }
 
 // Bounded-wait timeouts of this library's kernels (0 in correct operation).
@@ -422,34 +436,55 @@ cudaError_t launch_bp_z0_runs_tma(const float* y, float* x, const float* angles,
 // multiple of RUN (class-1 runs span RUN rows).
 // With addend, the class-1 launch also adds addend (same layout as x) into the
 // rows it writes, after its own sums: x = (x + A^T y) + addend.
+// programmatic: the first launch directly follows another run launch of the
+// same call (launch_ex); the class-1 launch follows the class-0 one.
 template <int R, bool FULL = false>
 cudaError_t launch_bp_z0_runs_h(const float* y, float* x, const float* angles, const Geom& g,
                                 int row_lo, int row_hi, cudaStream_t stream,
-                                const float* addend = nullptr) {
+                                const float* addend = nullptr, bool programmatic = false) {
   dim3 block(32, BPR_WARPS);
   const unsigned hchunks = ceil_div(g.H, 32 * R);
   const int nmaj0 = (int)ceil_div(g.SX, RUN);
   // class-0 runs in bands of RUN rows (run_origin): row_lo is a multiple of RUN
   const long long b0 = (long long)row_lo * nmaj0;
   const long long e0 = (long long)ceil_div(row_hi, RUN) * RUN * nmaj0;
+  const float* no_addend = nullptr;
   if (e0 > b0) {
-    bp_z0_runs_kernel<0, R, false, FULL><<<dim3(ceil_div(e0 - b0, BPR_WARPS), hchunks), block, 0,
-                                            stream>>>(
-        y, x, angles, g, nmaj0, (int)b0, (int)e0, row_hi, g.accumulate);
-    const cudaError_t e = cudaGetLastError();
+    const dim3 grid(ceil_div(e0 - b0, BPR_WARPS), hchunks);
+    cudaError_t e =
+        programmatic
+            ? launch_ex(bp_z0_runs_kernel<0, R, false, FULL, true>, grid, block, 0, stream,
+                        true, y, x, angles, g, nmaj0, (int)b0, (int)e0, row_hi, g.accumulate,
+                        no_addend)
+            : launch_ex(bp_z0_runs_kernel<0, R, false, FULL, false>, grid, block, 0, stream,
+                        false, y, x, angles, g, nmaj0, (int)b0, (int)e0, row_hi, g.accumulate,
+                        no_addend);
+    if (e == cudaSuccess) e = cudaGetLastError();
     if (e != cudaSuccess) return e;
+    programmatic = true;
   }
   const long long b1 = (long long)(row_lo / RUN) * g.SX;
   const long long e1 = (long long)ceil_div(row_hi, RUN) * g.SX;
   if (e1 > b1) {
     const dim3 grid(ceil_div(e1 - b1, BPR_WARPS), hchunks);
+    // the class-1 launch follows the class-0 one whenever there is one
+    cudaError_t e;
     if (addend)
-      bp_z0_runs_kernel<1, R, true, FULL><<<grid, block, 0, stream>>>(
-          y, x, angles, g, g.SX, (int)b1, (int)e1, row_hi, 1, addend);
+      e = programmatic ? launch_ex(bp_z0_runs_kernel<1, R, true, FULL, true>, grid, block, 0,
+                                   stream, true, y, x, angles, g, g.SX, (int)b1, (int)e1,
+                                   row_hi, 1, addend)
+                       : launch_ex(bp_z0_runs_kernel<1, R, true, FULL, false>, grid, block, 0,
+                                   stream, false, y, x, angles, g, g.SX, (int)b1, (int)e1,
+                                   row_hi, 1, addend);
     else
-      bp_z0_runs_kernel<1, R, false, FULL><<<grid, block, 0, stream>>>(
-          y, x, angles, g, g.SX, (int)b1, (int)e1, row_hi, 1);
-    return cudaGetLastError();
+      e = programmatic ? launch_ex(bp_z0_runs_kernel<1, R, false, FULL, true>, grid, block, 0,
+                                   stream, true, y, x, angles, g, g.SX, (int)b1, (int)e1,
+                                   row_hi, 1, no_addend)
+                       : launch_ex(bp_z0_runs_kernel<1, R, false, FULL, false>, grid, block,
+                                   0, stream, false, y, x, angles, g, g.SX, (int)b1, (int)e1,
+                                   row_hi, 1, no_addend);
+    if (e == cudaSuccess) e = cudaGetLastError();
+    return e;
   }
   return cudaSuccess;
 }
@@ -459,10 +494,12 @@ cudaError_t launch_bp_z0_runs_h(const float* y, float* x, const float* angles, c
 template <int R>
 cudaError_t launch_bp_z0_runs(const float* y, float* x, const float* angles, const Geom& g,
                               int row_lo, int row_hi, cudaStream_t stream,
-                              const float* addend = nullptr) {
+                              const float* addend = nullptr, bool programmatic = false) {
   if (R == 8 && g.H % (32 * 8) == 0)
-    return launch_bp_z0_runs_h<R, true>(y, x, angles, g, row_lo, row_hi, stream, addend);
-  return launch_bp_z0_runs_h<R, false>(y, x, angles, g, row_lo, row_hi, stream, addend);
+    return launch_bp_z0_runs_h<R, true>(y, x, angles, g, row_lo, row_hi, stream, addend,
+                                        programmatic);
+  return launch_bp_z0_runs_h<R, false>(y, x, angles, g, row_lo, row_hi, stream, addend,
+                                       programmatic);
 }
 
 // Runs with 8 heights per lane on heights [0, r8_heights(H)) and 4 on the
@@ -484,8 +521,10 @@ cudaError_t launch_bp_z0_runs_split(const float* y, float* x, const float* angle
   }
   Geom g4 = g;
   g4.H = g.H - H8;
+  // after the 8-height part's run launches (the bulk-copy form has no
+  // programmatic wait, so a launch after it is an ordinary one)
   return launch_bp_z0_runs<4>(y + H8, x + H8, angles, g4, row_lo, row_hi, stream,
-                              addend ? addend + H8 : nullptr);
+                              addend ? addend + H8 : nullptr, H8 > 0 && !tma);
 }
 
 bool bp0_vec4(const float* y, const float* x, const Geom& g) {

@@ -274,10 +274,13 @@ __device__ __forceinline__ void store_out(float* p, float v, int accumulate) {
 }
 
 // Epilogue whose read bypasses L1 (ld.global.cg): for outputs that another
-// block of the same launch wrote before signalling completion, since L1 is
-// not coherent across SMs.
-__device__ __forceinline__ void store_out_coherent(float4* p, float4 v) {
-  *p = f4_add(__ldcg(p), v);
+// block of the same launch, or the kernel before this one in a programmatic
+// launch, wrote while this block ran, since L1 is not coherent across SMs.
+__device__ __forceinline__ void store_out_coherent(float4* p, float4 v, int accumulate) {
+  *p = accumulate ? f4_add(__ldcg(p), v) : v;
+}
+__device__ __forceinline__ void store_out_coherent(float* p, float v, int accumulate) {
+  *p = accumulate ? __ldcg(p) + v : v;
 }
 
 // Epilogue of one lane's heights of the output row that starts at p.  With
@@ -291,13 +294,13 @@ __device__ __forceinline__ void store_lane(float* p, const LaneH<R>& lh,
     for (int k = 0; k < LaneH<R>::NQ; ++k) {
       if (lh.v[k]) {
         float4* q = reinterpret_cast<float4*>(p + lh.h + k * kSecondHalf);
-        if constexpr (COHERENT) store_out_coherent(q, parts[k]);
+        if constexpr (COHERENT) store_out_coherent(q, parts[k], accumulate);
         else store_out(q, parts[k], accumulate);
       }
     }
   } else if (lh.v[0]) {
     auto* q = reinterpret_cast<typename Vec<R>::T*>(p + lh.h);
-    if constexpr (COHERENT && R == 4) store_out_coherent(q, v); else store_out(q, v, accumulate);
+    if constexpr (COHERENT) store_out_coherent(q, v, accumulate); else store_out(q, v, accumulate);
   }
 }
 
@@ -313,7 +316,8 @@ __device__ __forceinline__ void add_lane(float* p, const float* a, const LaneH<R
       if (lh.v[k]) {
         float4* q = reinterpret_cast<float4*>(p + lh.h + k * kSecondHalf);
         const float4 c = __ldg(reinterpret_cast<const float4*>(a + lh.h + k * kSecondHalf));
-        const float4 t = with_v ? f4_add(*q, parts[k]) : *q;
+        const float4 o = __ldcg(q);  // possibly written by the previous launch (PdlWait)
+        const float4 t = with_v ? f4_add(o, parts[k]) : o;
         *q = f4_add(t, c);
       }
     }
@@ -321,10 +325,31 @@ __device__ __forceinline__ void add_lane(float* p, const float* a, const LaneH<R
     using V = typename Vec<R>::T;
     V* q = reinterpret_cast<V*>(p + lh.h);
     const V c = *reinterpret_cast<const V*>(a + lh.h);
-    const V t = with_v ? f4_add(*q, v) : *q;
+    const V o = __ldcg(q);
+    const V t = with_v ? f4_add(o, v) : o;
     *q = f4_add(t, c);
   }
 }
+
+// Programmatic dependent launch.  A kernel launched with programmatic stream
+// serialization (launch_ex) may start while the kernel before it in its
+// stream still runs.  pdl_trigger, run at the start of every block, lets such
+// a successor start once every block of this kernel has begun; PdlWait, run
+// by a warp just before it first reads back its outputs, holds until the
+// kernels this one depends on have completed and their writes are visible.
+// In a normally launched kernel, or one without a programmatic successor,
+// both return at once.
+__device__ __forceinline__ void pdl_trigger() {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+// (the wait makes those writes visible to this grid, so the read-back needs
+// no L1 bypass)
+struct PdlWait {
+  __device__ __forceinline__ void operator()() const {
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+  }
+  static constexpr bool coherent = false;
+};
 
 // Pre-store hook that does nothing (single-problem kernels).
 struct NoWait {

@@ -19,6 +19,7 @@
 #include <cuda_runtime.h>
 
 #include <atomic>
+#include <type_traits>
 
 #include "vp_common.cuh"
 #include "vp_fp_staged.cuh"
@@ -38,11 +39,15 @@ using namespace detail;
 // The 8-height, 4-bin form is held to 7 resident blocks per SM (72
 // registers), its fastest occupancy with 2 candidates in flight, and to 6
 // (80 registers, no spills) with 3 in flight.
+// PDL: the launch follows this call's previous slab launch programmatically
+// (launch_ex), so its warps wait for that launch before they add into y.
+// The first launch of a call keeps the form without the wait.
 // With SPLIT a block takes 2 bin runs instead of 4, each by 2 warps that
 // gather half of the slab's major lines each: twice the blocks, each half as
 // long, so the last wave of a launch leaves less of the GPU idle.  The first
 // half writes (in the caller's mode); after a block barrier the second adds.
-template <int R, int KW, bool AGROUP, int UN, bool SPLIT = false, bool FULL = false>
+template <int R, int KW, bool AGROUP, int UN, bool SPLIT = false, bool FULL = false,
+          bool PDL = false>
 __global__ void __launch_bounds__(32 * FP0_WARPS,
                                   SPLIT ? (R == 8 ? 7 : 8)
                                         : (R == 8 && KW == 4 ? (UN == 3 ? 6 : 7) : 0))
@@ -66,9 +71,13 @@ __global__ void __launch_bounds__(32 * FP0_WARPS,
                           HalfBarrier{second});
     if (!second) __syncthreads();  // the second half adds after this one wrote
   } else {
+    // a programmatic launch of the next slab may start as this one's last
+    // blocks run
+    pdl_trigger();
     const int p0 = (AGROUP ? blockIdx.x : blockIdx.x * FP0_WARPS + w) * KW;
     const int a = a_base + (AGROUP ? blockIdx.y * FP0_WARPS + w : blockIdx.y);
-    fp_z0_warp<R, KW, UN, NoWait, FULL>(x, y, angles, g, p0, a, h, slab, accumulate, cand[w]);
+    using Wait = std::conditional_t<PDL, PdlWait, NoWait>;
+    fp_z0_warp<R, KW, UN, Wait, FULL>(x, y, angles, g, p0, a, h, slab, accumulate, cand[w]);
   }
 }
 
@@ -337,6 +346,9 @@ struct SlabLaunch {
   Slab slab;
   int accumulate;
   int a_lo, a_hi;
+  // the launch directly follows this call's previous slab launch on the
+  // stream: it may start while that one runs (launch_ex)
+  bool programmatic = false;
 };
 
 template <int R, int KW, bool AGROUP, int UN, bool SPLIT = false, bool FULL = false>
@@ -352,11 +364,24 @@ cudaError_t launch_slab(const SlabLaunch& L, cudaStream_t stream, int* launches)
                                 : ceil_div(g.PX, KW * FP0_WARPS);
     const unsigned gy = AGROUP ? ceil_div(na, FP0_WARPS) : (unsigned)na;
     dim3 grid(gx, gy, ceil_div(g.H, 32 * R));
-    fp_z0_kernel<R, KW, AGROUP, UN, SPLIT, FULL><<<grid, block, 0, stream>>>(L.x, L.y, L.angles, g,
-                                                                (int)a_base, L.slab,
-                                                                L.accumulate);
+    // Programmatic launches for the default 8-height form only: the wait
+    // leaves its code as it was, where it costs the 4-height form 8 registers
+    // and some of the opt-in forms spills.
+    constexpr bool kPdlForm = R == 8 && KW == 4 && AGROUP && UN == 2 && !SPLIT;
+    cudaError_t e;
+    if constexpr (kPdlForm) {
+      if (L.programmatic || a_base > L.a_lo)
+        e = launch_ex(fp_z0_kernel<R, KW, AGROUP, UN, SPLIT, FULL, true>, grid, block, 0, stream,
+                      true, L.x, L.y, L.angles, g, (int)a_base, L.slab, L.accumulate);
+      else
+        e = launch_ex(fp_z0_kernel<R, KW, AGROUP, UN, SPLIT, FULL, false>, grid, block, 0,
+                      stream, false, L.x, L.y, L.angles, g, (int)a_base, L.slab, L.accumulate);
+    } else {
+      e = launch_ex(fp_z0_kernel<R, KW, AGROUP, UN, SPLIT, FULL, false>, grid, block, 0, stream,
+                    false, L.x, L.y, L.angles, g, (int)a_base, L.slab, L.accumulate);
+    }
     if (launches) ++*launches;
-    const cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaGetLastError();
     if (e != cudaSuccess) return e;
   }
   return cudaSuccess;
@@ -494,7 +519,7 @@ cudaError_t launch_fp_z0_config(const float* x, float* y, const float* angles, c
   const int nslabs = fp0_slabs(g, c);
   for (int k = k0; k < k1 && k < nslabs; ++k) {
     const SlabLaunch L{x, y, angles, g, fp0_slab(g, c, k, nslabs), k == 0 ? g.accumulate : 1,
-                       0, g.n_ang};
+                       0, g.n_ang, k > k0};
     const cudaError_t e = launch_slab_config(c, L, stream, launches);
     if (e != cudaSuccess) return e;
   }

@@ -9,6 +9,30 @@
 
 namespace vp {
 
+// Launches kernel k; with programmatic set, with programmatic stream
+// serialization, so that it may start while the kernel before it in the
+// stream still runs (the kernel must run PdlWait, vp_common.cuh, before it
+// reads back outputs that kernel writes).  Set only on a launch that directly
+// follows one of this library's own kernels in the same call: the kernel
+// before may then be running, but every operation before that one is done.
+template <typename... KArgs, typename... Args>
+cudaError_t launch_ex(void (*k)(KArgs...), dim3 grid, dim3 block, size_t smem,
+                      cudaStream_t stream, bool programmatic, Args&&... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = stream;
+  cudaLaunchAttribute attr[1];
+  if (programmatic) {
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+  }
+  return cudaLaunchKernelEx(&cfg, k, static_cast<KArgs>(args)...);
+}
+
 // y (z_order 0: (n_ang, PX, Hy), z_order 2: (Hy, n_ang, PX)) += A x.
 cudaError_t launch_forward_z0(const float* x, float* y, const float* angles, const Geom& g,
                               cudaStream_t stream);

@@ -192,15 +192,20 @@ VP_API int vp_forward_z2_noalloc(const float* x, int64_t x0, int64_t x1, int64_t
  * same variant, bit for bit. */
 #define VP_OP_FORWARD 0   /* out (y) += A in (x) */
 #define VP_OP_BACKWARD 1  /* out (x) += A^T in (y) */
+/* The single-problem forward variant that a batched forward problem of
+ * variant 0 runs: four neighbouring angles per block and 128 MB class slabs.
+ * Batched, its fewer stages wait less than the single-problem default's
+ * 64 MB slabs. */
+#define VP_BATCH_FORWARD_DEFAULT 21
 
 typedef struct vp_batch_problem {
   int op;                 /* VP_OP_FORWARD or VP_OP_BACKWARD */
   int flags;              /* VP_FLAG_* as for the single-problem calls */
   int variant;            /* the single-problem kernel variant whose body,
                              heights per lane and slabs the problem uses.
-                             Forward: 0 (the single-problem default) or
+                             Forward: 0 (= VP_BATCH_FORWARD_DEFAULT) or
                              any variant with 4 bins per warp (1, 3, 5, 7, 9,
-                             10, 11, 12, 16, 21).  Adjoint: 0 / 7 = runs in two angle
+                             10, 11, 12, 16, 21, 22, 23).  Adjoint: 0 / 7 = runs in two angle
                              classes, 8 heights per lane past 128 heights
                              (default); 6 = runs, 4 heights per lane; 4 = 2x2
                              voxel blocks (accumulates in the reference's

@@ -11,7 +11,7 @@ from oracle import oracle
 from tests import tolerances as tol
 from tests.common import lin, rel_err, seeded
 from voxelproj_gb300 import _lib
-from voxelproj_gb300.batch import Batch, uneven_cubes
+from voxelproj_gb300.batch import FORWARD_DEFAULT, Batch, uneven_cubes
 
 pytestmark = pytest.mark.gpu
 
@@ -31,7 +31,7 @@ def _inputs(geoms, seed):
 
 
 @pytest.mark.parametrize("vf,vb", [(1, 4), (1, 6), (0, 0), (10, 7), (5, 6), (12, 7), (21, 7),
-                                   (16, 6), (3, 4)])
+                                   (16, 6), (3, 4), (22, 7)])
 def test_batch_matches_single_problem_calls(vf, vb):
     """Same bodies, same slabs and stages, same order: the batch reproduces the
     single-problem kernels of the same variant bit for bit."""
@@ -49,8 +49,9 @@ def test_batch_matches_single_problem_calls(vf, vb):
     b.run()
     torch.cuda.synchronize()
     assert not b.error()
-    # the single-problem kernels of the same variants
-    _lib.LIB.vp_set_kernel_variant(0, vf)
+    # the single-problem kernels of the same variants (a batched forward of
+    # variant 0 runs FORWARD_DEFAULT)
+    _lib.LIB.vp_set_kernel_variant(0, vf or FORWARD_DEFAULT)
     _lib.LIB.vp_set_kernel_variant(1, vb)
     try:
         for c, (yo, xo) in zip(cases, outs):
@@ -90,7 +91,10 @@ def test_batch_stages_on_large_problems():
     b.run()  # runs accumulate: every output is now twice the operator
     torch.cuda.synchronize()
     assert not b.error()
-    try:  # default variants on both sides
+    # default variants on both sides: the batch's forward default is
+    # FORWARD_DEFAULT
+    _lib.LIB.vp_set_kernel_variant(0, FORWARD_DEFAULT)
+    try:
         for x, y, yo, xo, a in refs:
             ys = torch.zeros_like(yo)
             xs = torch.zeros_like(xo)
@@ -212,12 +216,16 @@ def test_batch_update_replans_in_place():
         return probs, outs
 
     def check(outs):
-        for x, y, a, yo, xo in outs:
-            ys, xs = torch.zeros_like(yo), torch.zeros_like(xo)
-            vp._CU.forward_z0(x, ys, a)
-            vp._CU.backward_z0(y, xs, a)
-            torch.cuda.synchronize()
-            assert torch.equal(yo, ys) and torch.equal(xo, xs)
+        _lib.LIB.vp_set_kernel_variant(0, FORWARD_DEFAULT)
+        try:
+            for x, y, a, yo, xo in outs:
+                ys, xs = torch.zeros_like(yo), torch.zeros_like(xo)
+                vp._CU.forward_z0(x, ys, a)
+                vp._CU.backward_z0(y, xs, a)
+                torch.cuda.synchronize()
+                assert torch.equal(yo, ys) and torch.equal(xo, xs)
+        finally:
+            _lib.LIB.vp_set_kernel_variant(0, 0)
 
     p1, o1 = make([2])
     b = Batch(p1)

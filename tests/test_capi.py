@@ -104,6 +104,14 @@ def test_batch_validation_without_gpu():
     assert lib.vp_batch_destroy(None) == _lib.VP_OK
 
 
+def test_batch_forward_default_matches_header():
+    from voxelproj_gb300 import batch
+
+    text = (ROOT / "include" / "voxelproj_gb300.h").read_text()
+    m = re.search(r"#define VP_BATCH_FORWARD_DEFAULT (\d+)", text)
+    assert m and int(m.group(1)) == batch.FORWARD_DEFAULT
+
+
 def test_batch_problem_layout_matches_header():
     # int op, flags, variant, reserved; 3 pointers; n_angles; 2 x int64[3]
     assert ctypes.sizeof(_lib.BatchProblem) == 16 + 3 * 8 + 8 + 48

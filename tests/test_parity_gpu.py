@@ -187,7 +187,7 @@ def test_backward_variants_store_mode_via_z2(variant, H):
 
 
 @pytest.mark.parametrize("variant", [1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12, 13, 14, 15, 16, 17,
-                                     19, 21])
+                                     19, 21, 22, 23])
 @pytest.mark.parametrize("geom", [(23, 37, 132, 61, 50, "wide"), (9, 6, 8, 40, 11, "axes"),
                                   (70, 64, 256, 96, 90, "rand"), (30, 21, 260, 33, 40, "rand"),
                                   (26, 31, 1024, 23, 36, "wide")],

@@ -24,7 +24,7 @@ import torch
 import voxelproj_gb300 as vp
 from tests.common import lin, seeded
 from voxelproj_gb300 import _lib
-from voxelproj_gb300.batch import Batch
+from voxelproj_gb300.batch import FORWARD_DEFAULT, Batch
 
 pytestmark = pytest.mark.gpu
 
@@ -74,13 +74,17 @@ def test_batch_stage_waits_run_out_and_report():
     b2.run()
     torch.cuda.synchronize()
     assert not b2.error()
-    for (x, y, a), yo, xo in zip(refs, outs[0::2], outs[1::2]):
-        ys = torch.zeros_like(yo)
-        xs = torch.zeros_like(xo)
-        vp._CU.forward_z0(x, ys, a)
-        vp._CU.backward_z0(y, xs, a)
-        torch.cuda.synchronize()
-        assert torch.equal(yo, ys) and torch.equal(xo, xs)
+    _lib.LIB.vp_set_kernel_variant(0, FORWARD_DEFAULT)  # the batch's forward default
+    try:
+        for (x, y, a), yo, xo in zip(refs, outs[0::2], outs[1::2]):
+            ys = torch.zeros_like(yo)
+            xs = torch.zeros_like(xo)
+            vp._CU.forward_z0(x, ys, a)
+            vp._CU.backward_z0(y, xs, a)
+            torch.cuda.synchronize()
+            assert torch.equal(yo, ys) and torch.equal(xo, xs)
+    finally:
+        _lib.LIB.vp_set_kernel_variant(0, 0)
     b2.close()
 
 

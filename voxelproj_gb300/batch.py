@@ -9,7 +9,8 @@ Each problem is (op, in, out, angles[, variant]): op "forward" adds A in to
 out, "backward" adds A^T in to out.  The tensors are CUDA float32 in z_order 0
 layout (x (SY, SX, H), y (n_ang, PX, H)) with H a multiple of 4; the batch
 keeps references to them.  Variants are single-problem kernel variants
-(None: the library default; the benchmark below asks the autotuner) and
+(None: the library default, for the forward FORWARD_DEFAULT; the benchmark
+below asks the autotuner) and
 select each problem's work-item body, heights per lane and volume slabs, so
 a batched problem's result equals the single-problem call of that variant.
 A body is the forward or the run adjoint with 4 or 8 heights per lane; each
@@ -36,6 +37,11 @@ import torch
 from . import _lib
 
 _OPS = {"forward": _lib.VP_OP_FORWARD, "backward": _lib.VP_OP_BACKWARD}
+
+# The single-problem forward variant that a batched forward problem of variant
+# 0 (or None) runs, VP_BATCH_FORWARD_DEFAULT in the C header: its results
+# equal single-problem calls of this variant bit for bit.
+FORWARD_DEFAULT = 21
 
 
 def _problem(op, inp, out, angles, variant):
@@ -151,6 +157,9 @@ def main() -> None:
                     help="explicit cubes as side:angles,... instead of the seeded workload")
     ap.add_argument("--only", choices=("both", "forward", "backward"), default="both",
                     help="batch A of every cube, A^T of every sinogram, or both")
+    ap.add_argument("--forward-variant", type=int, default=None,
+                    help="forward kernel variant of every problem, batched and sequential "
+                         "(default: the autotuner's, or the library default with --no-tune)")
     args = ap.parse_args()
     from . import _CU, tune
 
@@ -169,7 +178,8 @@ def main() -> None:
         y = torch.randn(n, side, side, device=dev, generator=g)
         y_out = torch.zeros(n, side, side, device=dev)
         x_out = torch.zeros(side, side, side, device=dev)
-        vf = None if args.no_tune else tune.batch_variant("forward", side, n)
+        vf = (args.forward_variant if args.forward_variant is not None
+              else None if args.no_tune else tune.batch_variant("forward", side, n))
         vb = None if args.no_tune else tune.batch_variant("backward", side, n)
         if fwd:
             problems.append(("forward", x, y_out, ang, vf))
@@ -202,10 +212,16 @@ def main() -> None:
             if bwd:
                 _CU.backward_z0(y, x_out, ang)
 
-    t_seq = timed(sequential)
-    before = _lib.LIB.vp_launch_count()
-    sequential()
-    seq_launches = _lib.LIB.vp_launch_count() - before
+    if args.forward_variant is not None:  # the sequential calls run it too
+        _lib.LIB.vp_set_kernel_variant(0, args.forward_variant)  # op 0: forward z0
+    try:
+        t_seq = timed(sequential)
+        before = _lib.LIB.vp_launch_count()
+        sequential()
+        seq_launches = _lib.LIB.vp_launch_count() - before
+    finally:
+        if args.forward_variant is not None:
+            _lib.LIB.vp_set_kernel_variant(0, 0)
     print(json.dumps({
         "workload": (f"cubes {args.cubes}" if args.cubes else
                      f"{args.count} cubes, sides {{64..384 step 32}}, U{{90..720}} angles each")

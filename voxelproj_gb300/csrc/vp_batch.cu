@@ -227,6 +227,16 @@ __device__ __forceinline__ void run_bwd_runs_item(const BatchDesc& d, int stage,
 // Each instance gets the register allocation of its single-problem kernel, so
 // no body runs at another body's occupancy; a plan launches the instances of
 // the bodies it holds, one persistent launch each.
+// Forward variant of a batched problem that asks for the default (0):
+// VP_BATCH_FORWARD_DEFAULT = 21, the single-problem default's angle groups
+// (in the 4-height form too) with 128 MB class slabs, whose fewer stages wait
+// less in a batch.  On the 64-cube
+// workload the batched forward took 151.5 ms with them against 154.8 ms with
+// the single-problem default's 64 MB slabs (sequential calls: 156.4 ms); the
+// single-problem calls gain more from 64 MB slabs, whose extra launches
+// overlap there.
+constexpr int kBatchForwardDefault = VP_BATCH_FORWARD_DEFAULT;
+
 constexpr int B_FWD4 = 0, B_FWD8 = 1, B_BWD4 = 2, B_BWD8 = 3, B_FWD8F = 4, B_BWD8F = 5,
               NBODIES = 6;
 
@@ -414,8 +424,10 @@ int part_desc(const vp_batch_problem& p, const vp::Geom& g, const float* in, flo
   d->out = out;
   d->angles = p.angles;
   if (p.op == VP_OP_FORWARD) {
-    // the single-problem forward's plan for this variant (0: its default)
-    const vp::Fp0Plan pl = vp::forward_z0_plan(g, true, p.variant);
+    // the single-problem forward's plan for this variant (0: the batch's
+    // default, kBatchForwardDefault)
+    const vp::Fp0Plan pl =
+        vp::forward_z0_plan(g, true, p.variant ? p.variant : vp::kBatchForwardDefault);
     if (pl.KW != 4 || pl.split || pl.staged ||
         (pl.R == 8 ? pl.un != 2 : pl.un != vp::detail::FP0_UNROLL))
       return VP_ERR_BATCH;  // bodies the batch does not carry
@@ -498,7 +510,7 @@ int batch_desc(const vp_batch_problem& p, std::vector<vp::BatchDesc>* out) {
   // heights per lane of the first part
   int R = 4;
   if (fwd)
-    R = vp::forward_z0_plan(g, true, p.variant).R;
+    R = vp::forward_z0_plan(g, true, p.variant ? p.variant : vp::kBatchForwardDefault).R;
   else if ((p.variant == 0 || p.variant == 7) && H > 128)
     R = 8;
   const int H8 = R == 8 ? vp::r8_heights(g.H) : g.H;

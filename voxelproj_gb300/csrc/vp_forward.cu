@@ -237,18 +237,22 @@ struct Fp0Config {
 // candidates in flight at 6 blocks per SM; 16 = as 10 with the warps of a
 // block on neighbouring angles; 17 = as 10, four aligned neighbouring angles
 // per block, the volume staged through shared memory by tensor copies
-// (vp_fp_staged.cuh); 19 = the aligned angle groups with plain loads; 21 =
-// as 16 with 128 MB slabs.  The default (0) is 21 with 8 heights per lane
-// and 10's layout (neighbouring bins) in the 4-height form.  Measured A per
-// call, variants 10 / 21: 512^3 and 192 angles 7.167 / 6.950 ms; 1024
-// angles 35.46 / 34.30 ms; 256^3 and 360 angles 1.685 / 1.583 ms; 384^3
-// and 641 angles 10.71 / 10.67 ms.  Heights not in float4 run the scalar form of
+// (vp_fp_staged.cuh); 19 = the aligned angle groups with plain loads; 21 /
+// 22 / 23 = as 16 with 128 / 32 / 256 MB slabs.  The default (0) is 16 with
+// 8 heights per lane and 10's layout (neighbouring bins) in the 4-height
+// form.  Measured A per call with programmatic launches between the slab
+// launches, variants 16 / 21 / 22 / 23: 512^3 and 192 angles 6.66 / 6.73 /
+// 7.05 / 7.12 ms; 1024 angles 32.98 / 33.89 / 35.06 ms; 256^3 and 360 angles
+// 1.534 / 1.585 / 1.551 ms; 384^3 and 641 angles 10.54 / 10.50 / 11.01 ms.
+// (Without them 21 led: 6.94 against 7.02 ms at 512^3, the extra slab
+// launches' tails costing more than the volume's better L2 residency.)
+// Heights not in float4 run the scalar form of
 // the same bin layout; 8-height variants on problems of at most 128 heights
 // run the 4-height form.
 Fp0Config fp0_config(const Geom& g, bool vec4, int variant) {
   Fp0Config c{vec4 ? 4 : 1, 4, false, FP0_UNROLL, 32, false, false, 0};
   const bool dflt = variant == 0;
-  if (dflt) variant = 21;  // the default
+  if (dflt) variant = 16;  // the default
   switch (variant) {
     case 2: c.KW = 8; break;
     case 3: c.agroup = true; break;
@@ -268,6 +272,8 @@ Fp0Config fp0_config(const Geom& g, bool vec4, int variant) {
     case 17: c.R = 8; c.un = 2; c.cls = true; c.slab_mb = 64; c.staged = 1; break;
     case 19: c.R = 8; c.un = 2; c.cls = true; c.slab_mb = 64; c.staged = 2; break;
     case 21: c.R = 8; c.un = 2; c.cls = true; c.slab_mb = 128; c.agroup = true; break;
+    case 22: c.R = 8; c.un = 2; c.cls = true; c.slab_mb = 32; c.agroup = true; break;
+    case 23: c.R = 8; c.un = 2; c.cls = true; c.slab_mb = 256; c.agroup = true; break;
     default: break;
   }
   if (c.R == 8 && (!vec4 || g.H <= 128)) {

@@ -27,8 +27,8 @@ import torch
 
 from . import _lib
 
-BATCH_CANDIDATES = {"forward": [21, 11, 10, 1], "backward": [7, 6, 4]}
-SINGLE_CANDIDATES = {"forward": [21, 10, 11, 16, 13, 7, 1], "backward": [7, 6, 4, 1]}
+BATCH_CANDIDATES = {"forward": [16, 21, 10, 1], "backward": [7, 6, 4]}
+SINGLE_CANDIDATES = {"forward": [16, 21, 10, 11, 13, 7, 1], "backward": [7, 6, 4, 1]}
 TUNE_ANGLES = 90
 
 

@@ -83,7 +83,8 @@ struct BatchDesc {
   int kind;
   int R;                // heights per lane: 4, or 8 as two float4 128 apart
   int nstages;          // stages per chunk
-  int counter_base;     // first counter of this problem (forward: per tile; adjoints: per stage)
+  int counter_base;     // first counter of this problem (forward: per tile; run adjoint:
+                        // per class-0 item; block adjoint: per stage, unused)
   // forward: slab plan (class slabs, rows and columns per slab); an item
   // row is an angle (its bins in groups of 4 runs, one per warp) or, with
   // agroup, a group of 4 neighbouring angles (one per warp, on the same
@@ -194,29 +195,39 @@ __device__ __noinline__ void run_fwd_item(const BatchDesc& d, int stage, int in_
   signal_done(slot->counter);
 }
 
+// A class-0 item (group grp) is the 4 x 4 voxel tile of band grp / nmaj
+// (rows 4 * band ..) and columns 4 * (grp % nmaj) .., one row per warp
+// (run_origin<0>); its counter counts its warps done.  A class-1 run (column
+// x, band b) adds into the 4 voxels that class-0 group b * nmaj + x / 4 wrote,
+// so each class-1 warp waits for that group alone (with columns a multiple of
+// 4, class-1 group g waits for class-0 group g).  Before, class-1 items
+// waited for every class-0 item of their height chunk, and the blocks that
+// took a chunk's first class-1 items spun while its last class-0 items ran.
 // FULL: the part's heights are whole 256-height chunks (R = 8).
 template <int R, bool FULL>
 __device__ __forceinline__ void run_bwd_runs_item(const BatchDesc& d, int stage, int grp,
                                                   int hc, RunsSmem& sm, int w, int lane,
                                                   unsigned* counters, int* error,
                                                   const WaitLimits& lim) {
-  unsigned* ctr = counters + d.counter_base + hc * d.nstages + stage;
+  unsigned* tiles = counters + d.counter_base + (size_t)hc * d.groups0;
   const int run = grp * BATCH_WARPS + w;
   const int h = hc * 32 * R + lane * 4;
+  const int nmaj = (d.g.SX + RUN - 1) / RUN;
   if (stage == 0) {
     int xi0, yi0;
-    run_origin<0>(run, (d.g.SX + RUN - 1) / RUN, &xi0, &yi0);
+    run_origin<0>(run, nmaj, &xi0, &yi0);
     if (run < d.nruns0 && yi0 < d.g.SY)
       bp_runs_warp<0, R, NoWait, false, FULL>(d.in, d.out, d.angles, d.g, xi0, yi0, h, 1,
                                               sm.tab[w], sm.alist[w]);
+    signal_done(tiles + grp);
   } else if (run < d.nruns1) {
-    const StageWait wt{ctr - 1, (unsigned)(d.groups0 * BATCH_WARPS) + lim.extra, error,
+    const int x = run % d.g.SX;
+    const int band = run / d.g.SX;
+    const StageWait wt{tiles + band * nmaj + x / RUN, (unsigned)BATCH_WARPS + lim.extra, error,
                        lim.spins};
-    bp_runs_warp<1, R, StageWait, false, FULL>(d.in, d.out, d.angles, d.g, run % d.g.SX,
-                                               (run / d.g.SX) * RUN, h, 1, sm.tab[w],
-                                               sm.alist[w], wt);
+    bp_runs_warp<1, R, StageWait, false, FULL>(d.in, d.out, d.angles, d.g, x, band * RUN, h, 1,
+                                               sm.tab[w], sm.alist[w], wt);
   }
-  signal_done(ctr);
 }
 
 // One kernel instance per body: the forward or the run adjoint with 4 or 8
@@ -467,8 +478,10 @@ int part_desc(const vp_batch_problem& p, const vp::Geom& g, const float* in, flo
   if (hch * d->per_chunk >= (1ll << 31)) return VP_ERR_BATCH;  // items indexed as int
   d->begin = hch * d->per_chunk;  // item count, turned into offsets later
   // counter count, turned into offsets later: one per forward tile, one per
-  // stage of the adjoints
-  const long long nctr = d->kind == vp::K_FWD ? hch * d->rows * d->units : hch * d->nstages;
+  // class-0 item of the run adjoint
+  const long long nctr = d->kind == vp::K_FWD        ? hch * d->rows * d->units
+                         : d->kind == vp::K_BWD_RUNS ? hch * d->groups0
+                                                     : hch * d->nstages;
   if (nctr >= (1ll << 31)) return VP_ERR_BATCH;
   d->counter_base = (int)nctr;
   return VP_OK;

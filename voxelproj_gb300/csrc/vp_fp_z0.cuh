@@ -50,8 +50,9 @@ __device__ __forceinline__ MinorRange minor_range(int i, float cent_major, float
 // candidate in it; class slabs give those angles a block of columns instead,
 // so every warp walks only the major lines of its slab.
 // With AGROUP the four warps of a block take four consecutive angles of the
-// same bins, so their voxel strips overlap near the rotation centre (L1 hits);
-// at 512^3 this measured slower than neighbouring bins.
+// same bins, so their voxel strips overlap near the rotation centre (L1 hits
+// of 46-58% at 512^3 against 10% for neighbouring bins): the default of the
+// 8-height form.  In the 4-height form neighbouring bins measured faster.
 // ---------------------------------------------------------------------------
 constexpr int FP0_WARPS = 4;
 constexpr int FP0_QBITS = 4;   // q in [0, KW + 1]

@@ -604,27 +604,26 @@ int launches_forward_z0(const float* x, const float* y, const Geom& g) {
 // the class slabs of the device path, spread over time.  The 4-height
 // remainder of a split heights range runs whole at the end
 // (launch_forward_z0_rest).
-// Pieces of at most 64 MB of one height chunk: pieces are copy and overlap
-// units as well as slabs, and smaller ones start the kernels sooner.
-constexpr int kStreamPieceMB = 64;
-
-int forward_z0_stream_rows(const float* x, const float* y, const Geom& g) {
+// Pieces of at most piece_mb MB of one height chunk (the caller's choice,
+// and no more than the plan's slabs): pieces are copy and overlap units as
+// well as slabs, and smaller ones start the kernels sooner.
+int forward_z0_stream_rows(const float* x, const float* y, const Geom& g, int piece_mb) {
   const bool vec4 = fp0_vec4(x, y, g);
   const int v = kernel_variant(OP_FORWARD_Z0);
   const Geom gm = fp0_parts(g, vec4, v).g[0];
   Fp0Config c = fp0_config(gm, vec4, v);
   c.cls = false;  // rows of one class alone: the row-slab budget
-  c.slab_mb = c.slab_mb < kStreamPieceMB ? c.slab_mb : kStreamPieceMB;
+  c.slab_mb = c.slab_mb < piece_mb ? c.slab_mb : piece_mb;
   return fp0_slab_rows(gm, c);
 }
 
-int forward_z0_stream_cols(const float* x, const float* y, const Geom& g) {
+int forward_z0_stream_cols(const float* x, const float* y, const Geom& g, int piece_mb) {
   const bool vec4 = fp0_vec4(x, y, g);
   const int v = kernel_variant(OP_FORWARD_Z0);
   const Geom gm = fp0_parts(g, vec4, v).g[0];
   Fp0Config c = fp0_config(gm, vec4, v);
   c.cls = false;
-  c.slab_mb = c.slab_mb < kStreamPieceMB ? c.slab_mb : kStreamPieceMB;
+  c.slab_mb = c.slab_mb < piece_mb ? c.slab_mb : piece_mb;
   Geom gt = gm;  // columns of the other class: rows and columns swapped
   gt.SY = gm.SX;
   gt.SX = gm.SY;

@@ -203,6 +203,10 @@ cudaError_t guarded(F body, cudaStream_t s) {
 // when adding; send puts the final angles [a0, a1) home (on the out stream),
 // the container added first.
 struct FwdZ0IO {  // z_order 0 host arrays: contiguous row and angle blocks
+  // volume pieces of at most this many MB of one height chunk (1-D copies):
+  // at 512^3 with 192 angles a call took 7.57 ms against 7.73 ms with 64 MB
+  // pieces, 7.80 with 24 or 48 and 7.87 with 16
+  static constexpr int piece_mb = 32;
   const float* x_host;
   float* y_host;
   const Geom& g;
@@ -232,6 +236,9 @@ struct FwdZ0IO {  // z_order 0 host arrays: contiguous row and angle blocks
 };
 
 struct FwdZ2IO {  // z_order 2 host arrays: strided blocks, transposed on the device
+  // pieces of at most 64 MB: smaller ones make more, narrower 2-D copies and
+  // transposes (3321 against 3437 GVU/s end to end with 32 MB pieces)
+  static constexpr int piece_mb = 64;
   const float* x_host;  // (H, SY, SX)
   float* y_host;        // (>= H, n_ang, PX): heights [0, H) are written
   const Geom& g2;       // the z_order 2 problem (its H heights)
@@ -274,8 +281,8 @@ cudaError_t forward_pipeline(const IO& io, const float* angles, const Geom& g, f
   // row pieces: a quarter slab, the rest of the first slab, then whole
   // slabs of the plan (which depends on the device buffers' alignment);
   // column pieces of the plan
-  const int rows = forward_z0_stream_rows(xd, yd, g);
-  const int cols = forward_z0_stream_cols(xd, yd, g);
+  const int rows = forward_z0_stream_rows(xd, yd, g, IO::piece_mb);
+  const int cols = forward_z0_stream_cols(xd, yd, g, IO::piece_mb);
   std::vector<int> cut{0};
   const int quarter = rows / 4 >= 8 ? rows / 4 : rows;
   int r = quarter < g.SY ? quarter : g.SY;

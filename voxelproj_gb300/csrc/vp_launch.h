@@ -119,8 +119,10 @@ Fp0Plan forward_z0_plan(const Geom& g, bool vec4, int variant);
 // 4-height remainder of a split heights range, whole), give the full result.
 // Adjoint: voxel rows [row_lo, row_hi) alone, row_lo a multiple of
 // backward_z0_row_step() (0: rows cannot be split, launch [0, SY) only).
-int forward_z0_stream_rows(const float* x, const float* y, const Geom& g);
-int forward_z0_stream_cols(const float* x, const float* y, const Geom& g);
+// Pieces hold at most piece_mb MB of one height chunk (and no more than the
+// forward plan's slabs).
+int forward_z0_stream_rows(const float* x, const float* y, const Geom& g, int piece_mb);
+int forward_z0_stream_cols(const float* x, const float* y, const Geom& g, int piece_mb);
 cudaError_t launch_forward_z0_stream(const float* x, float* y, const float* angles,
                                      const Geom& g, int rows_lo, int rows_hi, int cols_lo,
                                      int cols_hi, int a_lo, int a_hi, int accumulate,

@@ -7,7 +7,9 @@ import pytest
 import torch
 
 from tests.common import rel_err
+from voxelproj_gb300 import _lib
 from voxelproj_gb300.autograd import Projector
+from voxelproj_gb300.batch import FORWARD_DEFAULT
 from voxelproj_gb300.recon import ellipsoid_phantom, noisy_sinogram
 from voxelproj_gb300.serve import ReconstructionServer, Request, solve_plain
 
@@ -39,8 +41,15 @@ def test_results_same_alone_in_mix_and_plain():
         alone = ReconstructionServer(budget_bytes=8 << 30)
         alone.submit(r)
         x_alone = alone.run()[0].x
-        plain = solve_plain(r)
-        torch.cuda.synchronize()
+        # plain calls of the forward variant the batch runs (these requests
+        # are all batched): the library's own default may take another form
+        # for small problems, whose sums differ in order
+        _lib.LIB.vp_set_kernel_variant(0, FORWARD_DEFAULT)
+        try:
+            plain = solve_plain(r)
+            torch.cuda.synchronize()
+        finally:
+            _lib.LIB.vp_set_kernel_variant(0, 0)
         # identical arithmetic in all three: batched kernels reproduce the
         # single-problem ones and each request's elementwise steps are its own
         assert rel_err(done[r.rid].cpu().numpy(), x_alone.cpu().numpy()) <= 1e-6, spec

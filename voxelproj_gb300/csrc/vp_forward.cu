@@ -19,6 +19,7 @@
 #include <cuda_runtime.h>
 
 #include <atomic>
+#include <cmath>
 #include <type_traits>
 
 #include "vp_common.cuh"
@@ -249,6 +250,31 @@ struct Fp0Config {
 // Heights not in float4 run the scalar form of
 // the same bin layout; 8-height variants on problems of at most 128 heights
 // run the 4-height form.
+
+// Whether the default's 4-height form takes two warps per bin run (SPLIT),
+// for grids of less than two waves of blocks: when twice as many blocks of
+// half the work take fewer half-waves than the blocks take waves, or when
+// the blocks fill less than three quarters of one wave (smaller blocks then
+// balance the SMs better).  Measured A per call (192 angles, default /
+// split): 128^3 0.212 / 0.188 ms (1.26 waves of blocks); 96^3 0.114 /
+// 0.114-0.117 ms (0.95 waves); 64^3 0.073 / 0.067 ms (0.63 waves).
+// Without a device to ask, no.
+bool fp0_split_pays(const Geom& g) {
+  int dev = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+      sms <= 0) {
+    cudaGetLastError();
+    return false;
+  }
+  const double resident = 8.0 * sms;  // 4-height form: 8 blocks of 4 warps per SM
+  const double blocks = (double)ceil_div(g.PX, 4 * FP0_WARPS) *
+                        (g.n_ang < kMaxGridYZ ? g.n_ang : kMaxGridYZ) * ceil_div(g.H, 32 * 4);
+  const double w = blocks / resident;
+  if (w <= 0.0 || w >= 2.0) return false;
+  return std::ceil(2.0 * w) < 2.0 * std::ceil(w) || w <= 0.75;
+}
+
 Fp0Config fp0_config(const Geom& g, bool vec4, int variant) {
   Fp0Config c{vec4 ? 4 : 1, 4, false, FP0_UNROLL, 32, false, false, 0};
   const bool dflt = variant == 0;
@@ -282,8 +308,11 @@ Fp0Config fp0_config(const Geom& g, bool vec4, int variant) {
     c.staged = 0;
     // the default's 4-height form keeps neighbouring bins per block: angle
     // groups measured slower there (128^3, 192 angles: 0.223 against
-    // 0.2095 ms)
-    if (dflt) c.agroup = false;
+    // 0.2095 ms); with few blocks it splits each bin run over two warps
+    if (dflt) {
+      c.agroup = false;
+      c.split = vec4 && fp0_split_pays(g);
+    }
   }
   return c;
 }

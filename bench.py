@@ -491,15 +491,24 @@ def e2e_leg(args, vp, x_dev, ang_np, dev):
     for _ in range(min(args.warmup, 2)):
         step()
     torch.cuda.synchronize(dev)
-    k = max(1, min(args.steps, 5))
-    t0 = time.perf_counter()
+    # each step timed on its own (a step ends with its results in host
+    # memory); the median is reported, so that a stretch of host-side
+    # contention on a shared machine (seen to double single steps) does not
+    # decide the figure; mean and slowest step are reported beside it
+    k = max(5, min(args.steps, 10))
+    ts = []
     for _ in range(k):
+        t0 = time.perf_counter()
         step()
-    torch.cuda.synchronize(dev)
-    dt = (time.perf_counter() - t0) / k
+        torch.cuda.synchronize(dev)
+        ts.append(time.perf_counter() - t0)
+    dt = float(np.median(ts))
     vol, sino, a = 4 * S * S * H, 4 * n * S * H, 4 * n
     return {"value": round(2 * S * S * H * n / dt / 1e9, 3), "unit": UNIT,
-            "ms_per_step": round(dt * 1e3, 3),
+            "ms_per_step": round(dt * 1e3, 3), "steps_timed": k,
+            "stat": "median of individually timed steps",
+            "ms_per_step_mean": round(float(np.mean(ts)) * 1e3, 3),
+            "ms_per_step_max": round(float(np.max(ts)) * 1e3, 3),
             "h2d_bytes_per_step": vol + sino + a + sino + vol + a,
             "d2h_bytes_per_step": sino + vol,
             "path": "voxelproj_gb300.forward(x, angles, y) then backward(y, angles, x') with "

@@ -438,10 +438,13 @@ cudaError_t launch_bp_z0_runs_tma(const float* y, float* x, const float* angles,
 // rows it writes, after its own sums: x = (x + A^T y) + addend.
 // programmatic: the first launch directly follows another run launch of the
 // same call (launch_ex); the class-1 launch follows the class-0 one.
+// addend_ready: an event the class-1 launch, which reads addend, waits for
+// (the class-0 launch runs before the addend is in).
 template <int R, bool FULL = false>
 cudaError_t launch_bp_z0_runs_h(const float* y, float* x, const float* angles, const Geom& g,
                                 int row_lo, int row_hi, cudaStream_t stream,
-                                const float* addend = nullptr, bool programmatic = false) {
+                                const float* addend = nullptr, bool programmatic = false,
+                                cudaEvent_t addend_ready = nullptr) {
   dim3 block(32, BPR_WARPS);
   const unsigned hchunks = ceil_div(g.H, 32 * R);
   const int nmaj0 = (int)ceil_div(g.SX, RUN);
@@ -467,8 +470,14 @@ cudaError_t launch_bp_z0_runs_h(const float* y, float* x, const float* angles, c
   const long long e1 = (long long)ceil_div(row_hi, RUN) * g.SX;
   if (e1 > b1) {
     const dim3 grid(ceil_div(e1 - b1, BPR_WARPS), hchunks);
-    // the class-1 launch follows the class-0 one whenever there is one
+    // the class-1 launch follows the class-0 one whenever there is one (an
+    // ordinary launch after a wait for the addend)
     cudaError_t e;
+    if (addend && addend_ready) {
+      e = cudaStreamWaitEvent(stream, addend_ready, 0);
+      if (e != cudaSuccess) return e;
+      programmatic = false;
+    }
     if (addend)
       e = programmatic ? launch_ex(bp_z0_runs_kernel<1, R, true, FULL, true>, grid, block, 0,
                                    stream, true, y, x, angles, g, g.SX, (int)b1, (int)e1,
@@ -494,12 +503,13 @@ cudaError_t launch_bp_z0_runs_h(const float* y, float* x, const float* angles, c
 template <int R>
 cudaError_t launch_bp_z0_runs(const float* y, float* x, const float* angles, const Geom& g,
                               int row_lo, int row_hi, cudaStream_t stream,
-                              const float* addend = nullptr, bool programmatic = false) {
+                              const float* addend = nullptr, bool programmatic = false,
+                              cudaEvent_t addend_ready = nullptr) {
   if (R == 8 && g.H % (32 * 8) == 0)
     return launch_bp_z0_runs_h<R, true>(y, x, angles, g, row_lo, row_hi, stream, addend,
-                                        programmatic);
+                                        programmatic, addend_ready);
   return launch_bp_z0_runs_h<R, false>(y, x, angles, g, row_lo, row_hi, stream, addend,
-                                       programmatic);
+                                       programmatic, addend_ready);
 }
 
 // Runs with 8 heights per lane on heights [0, r8_heights(H)) and 4 on the
@@ -509,22 +519,26 @@ int bp0_split(const Geom& g) { return g.H > 128 ? r8_heights(g.H) : 0; }
 cudaError_t launch_bp_z0_runs_split(const float* y, float* x, const float* angles,
                                     const Geom& g, int row_lo, int row_hi,
                                     cudaStream_t stream, bool tma = false,
-                                    const float* addend = nullptr) {
+                                    const float* addend = nullptr,
+                                    cudaEvent_t addend_ready = nullptr) {
   const int H8 = bp0_split(g);
   if (H8 > 0) {
     Geom g8 = g;
     g8.H = H8;
     const cudaError_t e =
         tma ? launch_bp_z0_runs_tma(y, x, angles, g8, row_lo, row_hi, stream)
-            : launch_bp_z0_runs<8>(y, x, angles, g8, row_lo, row_hi, stream, addend);
+            : launch_bp_z0_runs<8>(y, x, angles, g8, row_lo, row_hi, stream, addend, false,
+                                   addend_ready);
     if (e != cudaSuccess || H8 == g.H) return e;
   }
   Geom g4 = g;
   g4.H = g.H - H8;
   // after the 8-height part's run launches (the bulk-copy form has no
-  // programmatic wait, so a launch after it is an ordinary one)
+  // programmatic wait, so a launch after it is an ordinary one); the addend
+  // wait was taken there, if there was one
   return launch_bp_z0_runs<4>(y + H8, x + H8, angles, g4, row_lo, row_hi, stream,
-                              addend ? addend + H8 : nullptr, H8 > 0 && !tma);
+                              addend ? addend + H8 : nullptr, H8 > 0 && !tma,
+                              H8 > 0 ? nullptr : addend_ready);
 }
 
 bool bp0_vec4(const float* y, const float* x, const Geom& g) {
@@ -600,11 +614,14 @@ bool backward_z0_rows_can_add(const float* y, const float* x, const Geom& g) {
 
 cudaError_t launch_backward_z0_rows_add(const float* y, float* x, const float* angles,
                                         const Geom& g, int row_lo, int row_hi,
-                                        const float* addend, cudaStream_t stream) {
+                                        const float* addend, cudaStream_t stream,
+                                        cudaEvent_t addend_ready) {
   if (!backward_z0_rows_can_add(y, x, g) || row_lo % RUN != 0) return cudaErrorInvalidValue;
   if (kernel_variant(OP_BACKWARD_Z0) == 6)
-    return launch_bp_z0_runs<4>(y, x, angles, g, row_lo, row_hi, stream, addend);
-  return launch_bp_z0_runs_split(y, x, angles, g, row_lo, row_hi, stream, false, addend);
+    return launch_bp_z0_runs<4>(y, x, angles, g, row_lo, row_hi, stream, addend, false,
+                                addend_ready);
+  return launch_bp_z0_runs_split(y, x, angles, g, row_lo, row_hi, stream, false, addend,
+                                 addend_ready);
 }
 
 cudaError_t launch_backward_z2(const float* y, float* x, const float* angles, const Geom& g,

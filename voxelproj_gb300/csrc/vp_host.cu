@@ -536,8 +536,10 @@ cudaError_t backward_pipeline(const IO& io, const float* angles, const Geom& g, 
     const int hi = lo + rows < g.SY ? lo + rows : g.SY;
     const cudaStream_t sk = (k & 1) ? c->compute2 : s;  // slabs write disjoint rows
     if (fused_add) {
-      VP_TRY(cudaStreamWaitEvent(sk, ev_cont[k], 0));
-      VP_TRY(launch_backward_z0_rows_add(yd + y0, xd, ad + a_split, g1, lo, hi, addend, sk));
+      // the slab's class-1 launch adds the container rows: only it waits
+      // for them, the class-0 launch starts as soon as the sinogram is in
+      VP_TRY(launch_backward_z0_rows_add(yd + y0, xd, ad + a_split, g1, lo, hi, addend, sk,
+                                         ev_cont[k]));
     } else {
       VP_TRY(launch_backward_z0_rows(yd + y0, xd, ad + a_split, g1, lo, hi, sk));
     }

@@ -148,11 +148,14 @@ cudaError_t launch_backward_z0_rows(const float* y, float* x, const float* angle
 // As launch_backward_z0_rows, and then adds addend (same layout as x) into
 // those rows: x = (x + A^T y) + addend in adding mode, A^T y + addend in
 // store mode, in the same order as a separate add after the projection.
-// Only for the run variants (backward_z0_rows_can_add).
+// Only for the run variants (backward_z0_rows_can_add).  addend_ready (may
+// be null): an event recorded once addend is in; the launches that read it
+// wait for it, the ones before them do not.
 bool backward_z0_rows_can_add(const float* y, const float* x, const Geom& g);
 cudaError_t launch_backward_z0_rows_add(const float* y, float* x, const float* angles,
                                         const Geom& g, int row_lo, int row_hi,
-                                        const float* addend, cudaStream_t stream);
+                                        const float* addend, cudaStream_t stream,
+                                        cudaEvent_t addend_ready = nullptr);
 
 // Host-buffer projections (vp_host.cu): g.accumulate selects out += result
 // (1) or out = result (0); *launches is incremented by the kernels launched.
